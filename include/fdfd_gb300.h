@@ -1,0 +1,180 @@
+/*
+ * fdfd_gb300.h — C ABI of the GB300 FDFD operator and solver.
+ *
+ * A drop-in for the hot path of MaxwellFDFD.jl: the sparse operator
+ *     A = Cₘ·(Pμ \ Cₑ) − ω²·Pε          (src/model/model.jl:248-250)
+ * that the reference assembles as a SparseMatrixCSC{ComplexF64} and the
+ * caller then applies (A*x, mul!(y,A,x)) or solves (A\b).  Here A is never
+ * assembled: it is applied matrix-free by sm_103a kernels.
+ *
+ * Conventions shared with the reference:
+ *   - complex numbers cross the boundary as interleaved (re, im) doubles
+ *     (Julia ComplexF64 memory layout);
+ *   - field vectors are component-fastest, DOF index c + 3·(i + Nx·(j + Ny·k))
+ *     (order_cmpfirst = true, model.jl:85, 88-94);
+ *   - the stretched ∆l arrays are the outputs of create_stretched_∆ls
+ *     (model.jl:135-152);
+ *   - the material tensor is the reference's εarr, an (Nx,Ny,Nz,3,3)
+ *     column-major ComplexF64 array (model.jl:64; full.jl:16-70).
+ *
+ * Every call returns an int status (FDFD_OK = 0); none aborts or traps.
+ * fdfd_last_error() returns the message of the last failure on a handle.
+ * A handle owns one CUDA stream and its device buffers; it must not be used
+ * from two threads at once.  Separate handles are independent.
+ */
+#ifndef FDFD_GB300_H
+#define FDFD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+enum {
+  FDFD_OK = 0,
+  FDFD_ERR_ARG = 1,           /* invalid argument: NULL pointer, bad size or enum   */
+  FDFD_ERR_UNSUPPORTED = 2,   /* valid model feature this build does not implement  */
+  FDFD_ERR_CUDA = 3,          /* CUDA runtime error                                  */
+  FDFD_ERR_NOMEM = 4,         /* device or pinned-host allocation failed             */
+  FDFD_ERR_NOT_CONVERGED = 5, /* solver reached maxit before tol                      */
+  FDFD_ERR_BREAKDOWN = 6,     /* Krylov breakdown (a recurrence scalar vanished)     */
+  FDFD_ERR_NO_DEVICE = 7,     /* no CUDA device                                       */
+  FDFD_ERR_NONFINITE = 8,     /* NaN/Inf met in the iteration                        */
+  FDFD_ERR_TIMEOUT = 9        /* a bounded device-side wait gave up                  */
+};
+
+/* arithmetic of an operator application */
+enum { FDFD_C128 = 0, FDFD_C64 = 1 };
+/* boundary field type (MaxwellBase EE / HH) */
+enum { FDFD_EE = 0, FDFD_HH = 1 };
+/* solver precision */
+enum { FDFD_PREC_FP64 = 0, FDFD_PREC_MIXED = 1 };
+/* Krylov method */
+enum { FDFD_BICGSTAB = 0, FDFD_COCG = 1 };
+
+typedef struct fdfd_handle fdfd_handle;
+
+/* Model description.  Replaces the inputs the reference feeds to
+ * create_curls / create_paramops (model.jl:154-188): grid size, boundary,
+ * Bloch phase, ω and the stretched ∆l arrays. */
+typedef struct {
+  int32_t N[3];             /* cells per axis                                          */
+  int32_t isbloch[3];       /* 1 = Bloch, 0 = symmetry boundary (PEC for boundft EE)   */
+  int32_t boundft[3];       /* FDFD_EE on every axis in this build                     */
+  int32_t order_cmpfirst;   /* must be 1                                               */
+  int32_t device;           /* CUDA device ordinal                                     */
+  int32_t reserved;
+  double omega[2];          /* ω (re, im)                                              */
+  double e_ikl[3][2];       /* e^{-i kbloch L} per axis (used on Bloch axes)           */
+  const double *sdl_e[3];   /* s∆lₑ: N[w] complex values at E-voxel-corner planes      */
+  const double *sdl_m[3];   /* s∆lₘ: N[w] complex values at H-voxel-corner planes      */
+} fdfd_desc;
+
+/* Shapes for the on-device assignment + subpixel smoothing of ε
+ * (replaces add_obj! + calc_matparams!, model.jl:120-133, full.jl:16-70). */
+enum { FDFD_SHAPE_SPHERE = 0, FDFD_SHAPE_BOX = 1 };
+typedef struct {
+  int32_t kind;     /* FDFD_SHAPE_*                                  */
+  int32_t pad;
+  double eps;       /* isotropic real ε of the object's material    */
+  double p[6];      /* sphere: cx, cy, cz, r; box: lox, loy, loz, hix, hiy, hiz */
+} fdfd_object;
+
+/* Optional per-cell ε design region over cells [lo, hi) (inverse design). */
+typedef struct {
+  int32_t lo[3];
+  int32_t hi[3];
+  const double *eps_cells;  /* (hi-lo) cells, x fastest                        */
+} fdfd_design;
+
+typedef struct {
+  int32_t method;           /* FDFD_BICGSTAB or FDFD_COCG                              */
+  int32_t precision;        /* FDFD_PREC_FP64 or FDFD_PREC_MIXED                       */
+  double tol;               /* target true relative residual ‖b − A x‖/‖b‖ (FP64)      */
+  int64_t maxit;            /* iteration cap                                           */
+  double delta;             /* mixed: reliable-update trigger (residual drop factor)   */
+  int32_t x0_given;         /* 1: x holds the initial guess                            */
+  int32_t check_every;      /* iterations per launched batch between host checks       */
+  int32_t transpose;        /* 1: solve Aᵀ x = b (adjoint)                             */
+  int32_t use_graph;        /* 1: replay each batch as a CUDA graph                     */
+} fdfd_solve_opts;
+
+typedef struct {
+  int64_t iterations;       /* Krylov iterations                                       */
+  int64_t matvecs;          /* operator applications (all precisions)                  */
+  int32_t refinements;      /* FP64 residual replacements (mixed)                      */
+  int32_t status;           /* FDFD_* status of the solve                              */
+  double relres;            /* final true FP64 relative residual                        */
+  double time_ms;           /* device time of the solve (CUDA events on the stream)    */
+} fdfd_stats;
+
+/* ---- lifetime ------------------------------------------------------------
+ * fdfd_create replaces create_linsys(EE, ω, create_paramops, create_curls, …)
+ * (model.jl:222-233) as the point where the operator comes into being. */
+int fdfd_create(const fdfd_desc *desc, fdfd_handle **out);
+void fdfd_destroy(fdfd_handle *h);
+const char *fdfd_last_error(const fdfd_handle *h);   /* h may be NULL        */
+const char *fdfd_version(void);
+void *fdfd_stream(fdfd_handle *h);                   /* the handle's cudaStream_t */
+int fdfd_sync(fdfd_handle *h);
+
+/* ---- material ------------------------------------------------------------
+ * Pε of create_paramops (model.jl:154-171).  εarr is the reference's
+ * (Nx,Ny,Nz,3,3) column-major ComplexF64 array: diagonal entries at the E_w
+ * samples, off-diagonal entries at E-voxel corners.  This build requires a
+ * real, symmetric tensor (lossless dielectric); other input returns
+ * FDFD_ERR_UNSUPPORTED. */
+int fdfd_set_eps_tensor(fdfd_handle *h, const double *epsarr);
+/* Compact form: eps_diag[c + 3·cell] = ε_cc at E_c; eps_off[p + 3·cell] =
+ * ε_xy, ε_yz, ε_zx at the corner of cell (NULL = no off-diagonal). */
+int fdfd_set_eps(fdfd_handle *h, const double *eps_diag, const double *eps_off);
+/* On-device assign + Kottke smoothing.  lprim[w] holds the N[w]+1 primal
+ * plane locations (both domain ends); objects are in add_obj! order (last
+ * wins); design may be NULL. */
+int fdfd_smooth_objects(fdfd_handle *h, const double *const lprim[3],
+                        const fdfd_object *objs, int32_t nobj, double eps_bg,
+                        const fdfd_design *design);
+/* Read back ε (compact form, doubles) and the smoothing mask
+ * smask[s + 4·cell] (s = Exx, Eyy, Ezz, corner; 0 assigned, 1 Kottke,
+ * 2 design).  Any pointer may be NULL. */
+int fdfd_get_eps(fdfd_handle *h, double *eps_diag, double *eps_off, uint8_t *smask);
+
+/* ---- operator application --------------------------------------------------
+ * y = A x (mul!(y, A, x) on the reference's assembled A, model.jl:238-259).
+ * Host buffers: 2·3·Ncell doubles (ComplexF64).  precision = FDFD_C64
+ * computes in complex64 (x rounded, y widened). */
+int fdfd_matvec(fdfd_handle *h, const double *x, double *y, int32_t precision);
+/* Device buffers on the handle's stream (asynchronous): double2 for
+ * FDFD_C128, float2 for FDFD_C64. */
+int fdfd_matvec_dev(fdfd_handle *h, const void *x, void *y, int32_t precision);
+/* y = Aᵀ x (transpose(A)*x; used by the adjoint). */
+int fdfd_matvec_transpose(fdfd_handle *h, const double *x, double *y, int32_t precision);
+
+/* ---- solve -----------------------------------------------------------------
+ * x = A \ b to a true relative residual opts->tol (the reference leaves this
+ * to Julia's A\b).  Host buffers, nrhs right-hand sides stored one after the
+ * other (each 2·3·Ncell doubles).  stats may be NULL or an array of nrhs. */
+int fdfd_solve(fdfd_handle *h, const double *b, double *x, int32_t nrhs,
+               const fdfd_solve_opts *opts, fdfd_stats *stats);
+/* Device buffers (double2, 3·Ncell each) on the handle's stream; returns
+ * after the solve completes. */
+int fdfd_solve_dev(fdfd_handle *h, const void *b, void *x,
+                   const fdfd_solve_opts *opts, fdfd_stats *stats);
+void fdfd_default_opts(fdfd_solve_opts *opts);
+
+/* ---- adjoint gradient --------------------------------------------------------
+ * For A e = b and a real objective L(e) with g = ∂L/∂e (holomorphic
+ * derivative, interleaved complex), solves Aᵀ λ = g and returns
+ * dL/dε_ww at every E_w sample: grad[c + 3·cell] = 2·ω²·Re(λ_c·e_c) ... as
+ * defined in the design notes (sign convention included).  e, g, grad are
+ * host buffers. */
+int fdfd_eps_grad(fdfd_handle *h, const double *e, const double *g, double *grad,
+                  const fdfd_solve_opts *opts, fdfd_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FDFD_GB300_H */

@@ -1,0 +1,301 @@
+// Vector kernels of the Krylov solvers: the BiCGSTAB / COCG updates with
+// their dot products fused in, precision conversions for the mixed
+// (complex64 + FP64 refinement) solver, and the reduction buffer.
+//
+// All reducing kernels use a fixed grid (RED_BLOCKS × 256 threads) and a
+// grid-stride loop, so the per-block partials and therefore the reduced
+// values are deterministic for a given problem size.
+#include "krylov_fin.cuh"
+
+namespace fdfd {
+
+constexpr int VB = 256;          // threads per block
+constexpr int RED_BLOCKS = 152 * 4;
+
+int ensure_red(fdfd_handle *h, int blocks) {
+  if (blocks < RED_BLOCKS) blocks = RED_BLOCKS;
+  if (h->red.part != nullptr && h->red_blocks >= blocks) return FDFD_OK;
+  if (h->red.part) cudaFree(h->red.part);
+  if (h->red.count) cudaFree(h->red.count);
+  h->red.part = nullptr;
+  h->red.count = nullptr;
+  cudaError_t e = cudaMalloc(&h->red.part, sizeof(double2) * 2 * (size_t)blocks);
+  if (e != cudaSuccess) return set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(reduction partials) failed");
+  e = cudaMalloc(&h->red.count, sizeof(unsigned int));
+  if (e != cudaSuccess) return set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(reduction counter) failed");
+  e = cudaMemsetAsync(h->red.count, 0, sizeof(unsigned int), h->stream);
+  if (e != cudaSuccess) return cuda_check(h, e, "cudaMemsetAsync(counter)");
+  h->red_blocks = blocks;
+  return FDFD_OK;
+}
+
+template <typename C> __device__ __forceinline__ C ld(const C *p, long long i) { return p[i]; }
+
+template <typename R>
+__device__ __forceinline__ typename CT<R>::C tocr(double2 v) {
+  return mk(R(v.x), R(v.y));
+}
+
+// p = r + β (p − ω v)
+template <typename R>
+__global__ void __launch_bounds__(VB) k_bicg_p(const typename CT<R>::C *__restrict__ r, typename CT<R>::C *p,
+                                               const typename CT<R>::C *__restrict__ v, long long n,
+                                               const KScalars *sc) {
+  using C = typename CT<R>::C;
+  if (sc->done) return;
+  const C be = tocr<R>(sc->beta), om = tocr<R>(sc->omega);
+  for (long long i = blockIdx.x * (long long)VB + threadIdx.x; i < n; i += (long long)gridDim.x * VB) {
+    const C t = csub(p[i], cmul(om, v[i]));
+    p[i] = cadd(r[i], cmul(be, t));
+  }
+}
+
+// s = r − α v
+template <typename R>
+__global__ void __launch_bounds__(VB) k_bicg_s(const typename CT<R>::C *__restrict__ r,
+                                               const typename CT<R>::C *__restrict__ v, typename CT<R>::C *s,
+                                               long long n, const KScalars *sc) {
+  using C = typename CT<R>::C;
+  if (sc->done) return;
+  const C al = tocr<R>(sc->alpha);
+  for (long long i = blockIdx.x * (long long)VB + threadIdx.x; i < n; i += (long long)gridDim.x * VB)
+    s[i] = csub(r[i], cmul(al, v[i]));
+}
+
+// x += α p + ω s;  r = s − ω t;  (r̂, r), ‖r‖²  → FIN_XR
+template <typename R>
+__global__ void __launch_bounds__(VB) k_bicg_xr(typename CT<R>::C *x, const typename CT<R>::C *__restrict__ p,
+                                                const typename CT<R>::C *__restrict__ s,
+                                                const typename CT<R>::C *__restrict__ t, typename CT<R>::C *r,
+                                                const typename CT<R>::C *__restrict__ rh, long long n, RedBuf red,
+                                                KScalars *sc) {
+  using C = typename CT<R>::C;
+  if (sc->done) return;
+  const C al = tocr<R>(sc->alpha), om = tocr<R>(sc->omega);
+  Acc<R> a0r, a0i, a1;
+  for (long long i = blockIdx.x * (long long)VB + threadIdx.x; i < n; i += (long long)gridDim.x * VB) {
+    const C si = s[i];
+    x[i] = cadd(x[i], cadd(cmul(al, p[i]), cmul(om, si)));
+    const C ri = csub(si, cmul(om, t[i]));
+    r[i] = ri;
+    const C d = cdotc(rh[i], ri);
+    a0r.add(d.x);
+    a0i.add(d.y);
+    a1.add(ri.x * ri.x + ri.y * ri.y);
+  }
+  block_reduce_finalise<VB>(make_double2(a0r.get(), a0i.get()), make_double2(a1.get(), 0.0), red, FIN_XR, sc);
+}
+
+// COCG (symmetric form, right-preconditioned by diagonal d):
+//   x += α p ; r −= α q ; rᵀ z and ‖r‖² with z = d∘r  → FIN_COCG_R
+template <typename R>
+__global__ void __launch_bounds__(VB) k_cocg_xr(typename CT<R>::C *x, const typename CT<R>::C *__restrict__ p,
+                                                const typename CT<R>::C *__restrict__ q, typename CT<R>::C *r,
+                                                const typename CT<R>::C *__restrict__ wgt, long long n, RedBuf red,
+                                                KScalars *sc) {
+  using C = typename CT<R>::C;
+  if (sc->done) return;
+  const C al = tocr<R>(sc->alpha);
+  Acc<R> a0r, a0i, a1;
+  for (long long i = blockIdx.x * (long long)VB + threadIdx.x; i < n; i += (long long)gridDim.x * VB) {
+    x[i] = cadd(x[i], cmul(al, p[i]));
+    const C ri = csub(r[i], cmul(al, q[i]));
+    r[i] = ri;
+    const C wr = cmul(wgt[i], ri);  // S r
+    const C d = cmul(ri, wr);       // rᵀ S r (unconjugated)
+    a0r.add(d.x);
+    a0i.add(d.y);
+    a1.add(ri.x * ri.x + ri.y * ri.y);
+  }
+  block_reduce_finalise<VB>(make_double2(a0r.get(), a0i.get()), make_double2(a1.get(), 0.0), red, FIN_COCG_R, sc);
+}
+
+// COCG direction: p = r + β p
+template <typename R>
+__global__ void __launch_bounds__(VB) k_cocg_p(const typename CT<R>::C *__restrict__ r, typename CT<R>::C *p,
+                                               long long n, const KScalars *sc) {
+  using C = typename CT<R>::C;
+  if (sc->done) return;
+  const C be = tocr<R>(sc->beta);
+  for (long long i = blockIdx.x * (long long)VB + threadIdx.x; i < n; i += (long long)gridDim.x * VB)
+    p[i] = cadd(r[i], cmul(be, p[i]));
+}
+
+// Generic reductions: mode 0: (a, b) Hermitian and ‖a‖²;  mode 1: aᵀ S a
+template <typename R>
+__global__ void __launch_bounds__(VB) k_dot(const typename CT<R>::C *__restrict__ a,
+                                            const typename CT<R>::C *__restrict__ b, long long n, RedBuf red,
+                                            KScalars *sc) {
+  using C = typename CT<R>::C;
+  Acc<R> a0r, a0i, a1;
+  for (long long i = blockIdx.x * (long long)VB + threadIdx.x; i < n; i += (long long)gridDim.x * VB) {
+    const C ai = a[i];
+    const C d = cdotc(ai, b[i]);
+    a0r.add(d.x);
+    a0i.add(d.y);
+    a1.add(ai.x * ai.x + ai.y * ai.y);
+  }
+  block_reduce_finalise<VB>(make_double2(a0r.get(), a0i.get()), make_double2(a1.get(), 0.0), red, FIN_NONE, sc);
+}
+
+// pᵀ (S q) (unconjugated, weighted) → FIN_COCG_A
+template <typename R>
+__global__ void __launch_bounds__(VB) k_dot_u(const typename CT<R>::C *__restrict__ a,
+                                              const typename CT<R>::C *__restrict__ b,
+                                              const typename CT<R>::C *__restrict__ wgt, long long n, RedBuf red,
+                                              int fin, KScalars *sc) {
+  using C = typename CT<R>::C;
+  if (fin != FIN_NONE && sc->done) return;
+  Acc<R> a0r, a0i;
+  for (long long i = blockIdx.x * (long long)VB + threadIdx.x; i < n; i += (long long)gridDim.x * VB) {
+    const C d = cmul(a[i], cmul(wgt[i], b[i]));
+    a0r.add(d.x);
+    a0i.add(d.y);
+  }
+  block_reduce_finalise<VB>(make_double2(a0r.get(), a0i.get()), make_double2(0.0, 0.0), red, fin, sc);
+}
+
+// ---------------------------------------------------------------- mixed precision
+// x64 += x32; x32 = 0
+__global__ void __launch_bounds__(VB) k_accum(double2 *x64, float2 *x32, long long n) {
+  for (long long i = blockIdx.x * (long long)VB + threadIdx.x; i < n; i += (long long)gridDim.x * VB) {
+    const float2 v = x32[i];
+    double2 a = x64[i];
+    a.x += (double)v.x;
+    a.y += (double)v.y;
+    x64[i] = a;
+    x32[i] = make_float2(0.f, 0.f);
+  }
+}
+// x64 += x (double) ; x = 0
+__global__ void __launch_bounds__(VB) k_accum64(double2 *x64, double2 *x, long long n) {
+  for (long long i = blockIdx.x * (long long)VB + threadIdx.x; i < n; i += (long long)gridDim.x * VB) {
+    const double2 v = x[i];
+    double2 a = x64[i];
+    a.x += v.x;
+    a.y += v.y;
+    x64[i] = a;
+    x[i] = make_double2(0.0, 0.0);
+  }
+}
+__global__ void __launch_bounds__(VB) k_demote(float2 *y, const double2 *__restrict__ x, long long n) {
+  for (long long i = blockIdx.x * (long long)VB + threadIdx.x; i < n; i += (long long)gridDim.x * VB) {
+    const double2 v = x[i];
+    y[i] = make_float2((float)v.x, (float)v.y);
+  }
+}
+__global__ void __launch_bounds__(VB) k_promote(double2 *y, const float2 *__restrict__ x, long long n) {
+  for (long long i = blockIdx.x * (long long)VB + threadIdx.x; i < n; i += (long long)gridDim.x * VB) {
+    const float2 v = x[i];
+    y[i] = make_double2((double)v.x, (double)v.y);
+  }
+}
+template <typename R>
+__global__ void __launch_bounds__(VB) k_copy(typename CT<R>::C *y, const typename CT<R>::C *__restrict__ x,
+                                             long long n) {
+  for (long long i = blockIdx.x * (long long)VB + threadIdx.x; i < n; i += (long long)gridDim.x * VB) y[i] = x[i];
+}
+template <typename R>
+__global__ void __launch_bounds__(VB) k_conj_copy(typename CT<R>::C *y, const typename CT<R>::C *__restrict__ x,
+                                                  long long n) {
+  for (long long i = blockIdx.x * (long long)VB + threadIdx.x; i < n; i += (long long)gridDim.x * VB) {
+    const auto v = x[i];
+    y[i] = mk(v.x, -v.y);
+  }
+}
+
+static inline int vgrid(long long n) {
+  long long b = (n + VB - 1) / VB;
+  if (b > RED_BLOCKS) b = RED_BLOCKS;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+// ------------------------------------------------------------------ launchers
+template <typename R>
+int bicg_p(fdfd_handle *h, const typename CT<R>::C *r, typename CT<R>::C *p, const typename CT<R>::C *v, long long n,
+           const KScalars *sc) {
+  k_bicg_p<R><<<vgrid(n), VB, 0, h->stream>>>(r, p, v, n, sc);
+  return cuda_check(h, cudaGetLastError(), "k_bicg_p");
+}
+template <typename R>
+int bicg_s(fdfd_handle *h, const typename CT<R>::C *r, const typename CT<R>::C *v, typename CT<R>::C *s, long long n,
+           const KScalars *sc) {
+  k_bicg_s<R><<<vgrid(n), VB, 0, h->stream>>>(r, v, s, n, sc);
+  return cuda_check(h, cudaGetLastError(), "k_bicg_s");
+}
+template <typename R>
+int bicg_xr(fdfd_handle *h, typename CT<R>::C *x, const typename CT<R>::C *p, const typename CT<R>::C *s,
+            const typename CT<R>::C *t, typename CT<R>::C *r, const typename CT<R>::C *rh, long long n, KScalars *sc) {
+  int rc = ensure_red(h, RED_BLOCKS);
+  if (rc) return rc;
+  k_bicg_xr<R><<<vgrid(n), VB, 0, h->stream>>>(x, p, s, t, r, rh, n, h->red, sc);
+  return cuda_check(h, cudaGetLastError(), "k_bicg_xr");
+}
+template <typename R>
+int cocg_xr(fdfd_handle *h, typename CT<R>::C *x, const typename CT<R>::C *p, const typename CT<R>::C *q,
+            typename CT<R>::C *r, const typename CT<R>::C *w, long long n, KScalars *sc) {
+  int rc = ensure_red(h, RED_BLOCKS);
+  if (rc) return rc;
+  k_cocg_xr<R><<<vgrid(n), VB, 0, h->stream>>>(x, p, q, r, w, n, h->red, sc);
+  return cuda_check(h, cudaGetLastError(), "k_cocg_xr");
+}
+template <typename R>
+int cocg_p(fdfd_handle *h, const typename CT<R>::C *r, typename CT<R>::C *p, long long n, const KScalars *sc) {
+  k_cocg_p<R><<<vgrid(n), VB, 0, h->stream>>>(r, p, n, sc);
+  return cuda_check(h, cudaGetLastError(), "k_cocg_p");
+}
+template <typename R>
+int dot(fdfd_handle *h, const typename CT<R>::C *a, const typename CT<R>::C *b, long long n, KScalars *sc) {
+  int rc = ensure_red(h, RED_BLOCKS);
+  if (rc) return rc;
+  k_dot<R><<<vgrid(n), VB, 0, h->stream>>>(a, b, n, h->red, sc);
+  return cuda_check(h, cudaGetLastError(), "k_dot");
+}
+template <typename R>
+int dot_u(fdfd_handle *h, const typename CT<R>::C *a, const typename CT<R>::C *b, const typename CT<R>::C *w,
+          long long n, int fin, KScalars *sc) {
+  int rc = ensure_red(h, RED_BLOCKS);
+  if (rc) return rc;
+  k_dot_u<R><<<vgrid(n), VB, 0, h->stream>>>(a, b, w, n, h->red, fin, sc);
+  return cuda_check(h, cudaGetLastError(), "k_dot_u");
+}
+int accum(fdfd_handle *h, double2 *x64, float2 *x32, long long n) {
+  k_accum<<<vgrid(n), VB, 0, h->stream>>>(x64, x32, n);
+  return cuda_check(h, cudaGetLastError(), "k_accum");
+}
+int accum64(fdfd_handle *h, double2 *x64, double2 *x, long long n) {
+  k_accum64<<<vgrid(n), VB, 0, h->stream>>>(x64, x, n);
+  return cuda_check(h, cudaGetLastError(), "k_accum64");
+}
+int demote(fdfd_handle *h, float2 *y, const double2 *x, long long n) {
+  k_demote<<<vgrid(n), VB, 0, h->stream>>>(y, x, n);
+  return cuda_check(h, cudaGetLastError(), "k_demote");
+}
+int promote(fdfd_handle *h, double2 *y, const float2 *x, long long n) {
+  k_promote<<<vgrid(n), VB, 0, h->stream>>>(y, x, n);
+  return cuda_check(h, cudaGetLastError(), "k_promote");
+}
+template <typename R>
+int copy(fdfd_handle *h, typename CT<R>::C *y, const typename CT<R>::C *x, long long n) {
+  k_copy<R><<<vgrid(n), VB, 0, h->stream>>>(y, x, n);
+  return cuda_check(h, cudaGetLastError(), "k_copy");
+}
+
+#define INST(R)                                                                                                      \
+  template int bicg_p<R>(fdfd_handle *, const CT<R>::C *, CT<R>::C *, const CT<R>::C *, long long, const KScalars *); \
+  template int bicg_s<R>(fdfd_handle *, const CT<R>::C *, const CT<R>::C *, CT<R>::C *, long long, const KScalars *); \
+  template int bicg_xr<R>(fdfd_handle *, CT<R>::C *, const CT<R>::C *, const CT<R>::C *, const CT<R>::C *,          \
+                          CT<R>::C *, const CT<R>::C *, long long, KScalars *);                                       \
+  template int cocg_xr<R>(fdfd_handle *, CT<R>::C *, const CT<R>::C *, const CT<R>::C *, CT<R>::C *,                 \
+                          const CT<R>::C *, long long, KScalars *);                                                   \
+  template int cocg_p<R>(fdfd_handle *, const CT<R>::C *, CT<R>::C *, long long, const KScalars *);                 \
+  template int dot<R>(fdfd_handle *, const CT<R>::C *, const CT<R>::C *, long long, KScalars *);                     \
+  template int dot_u<R>(fdfd_handle *, const CT<R>::C *, const CT<R>::C *, const CT<R>::C *, long long, int,        \
+                        KScalars *);                                                                                  \
+  template int copy<R>(fdfd_handle *, CT<R>::C *, const CT<R>::C *, long long);
+INST(float)
+INST(double)
+#undef INST
+
+}  // namespace fdfd

@@ -1,0 +1,525 @@
+// C ABI of libfdfd_gb300 (declared in include/fdfd_gb300.h).
+//
+// The reference's boundary for this path is the assembled operator and
+// right-hand side returned by create_linsys / create_A / create_b
+// (src/model/model.jl:222-287), consumed by A*x, mul!(y,A,x) and A\b.
+// Here the host passes the inputs of that assembly — the stretched ∆l of
+// create_stretched_∆ls (:135-152) and the material tensor εarr
+// (:64, full.jl:16-70) — once, and every application or solve runs on the
+// GPU against device-resident data.
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "krylov_fin.cuh"
+
+namespace fdfd {
+
+static thread_local std::string g_last_error;
+
+int set_error(fdfd_handle *h, int code, const std::string &msg) {
+  if (h) h->err = msg;
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_check(fdfd_handle *h, cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return FDFD_OK;
+  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) return set_error(h, FDFD_ERR_NOMEM, m);
+  return set_error(h, FDFD_ERR_CUDA, m);
+}
+
+int solve_dev_impl(fdfd_handle *h, const double2 *b, double2 *x, const fdfd_solve_opts *o, fdfd_stats *st);
+int demote(fdfd_handle *, float2 *, const double2 *, long long);
+int promote(fdfd_handle *, double2 *, const float2 *, long long);
+
+using cd = std::complex<double>;
+
+// S = V_E per DOF (the symmetriser of A): V_E(c) = s∆lₘ[c][g_c] Π_{v≠c} s∆lₑ[v][g_v]
+__global__ void k_weights(const double2 *coef, int st, int o0, int o1, int o2, int N0, int N1, int N2, double2 *w64,
+                          float2 *w32) {
+  const long long ncell = (long long)N0 * N1 * N2;
+  for (long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x; cell < ncell;
+       cell += (long long)gridDim.x * blockDim.x) {
+    const int g[3] = {(int)(cell % N0), (int)((cell / N0) % N1), (int)(cell / ((long long)N0 * N1))};
+    const int off[3] = {o0, o1, o2};
+    for (int c = 0; c < 3; ++c) {
+      double2 v = make_double2(1.0, 0.0);
+      for (int a = 0; a < 3; ++a) {
+        const double2 f = coef[(a == c ? 5 : 4) * st + off[a] + g[a]];
+        v = make_double2(v.x * f.x - v.y * f.y, v.x * f.y + v.y * f.x);
+      }
+      if (w64) w64[3 * cell + c] = v;
+      if (w32) w32[3 * cell + c] = make_float2((float)v.x, (float)v.y);
+    }
+  }
+}
+
+int build_weights(fdfd_handle *h, double2 *w64, float2 *w32) {
+  k_weights<<<152 * 4, 256, 0, h->stream>>>(h->coef64, h->coef_stride, (int)h->coef_off[0], (int)h->coef_off[1],
+                                            (int)h->coef_off[2], h->N[0], h->N[1], h->N[2], w64, w32);
+  return cuda_check(h, cudaGetLastError(), "k_weights");
+}
+
+// Flag (xy tile, plane k) if any off-diagonal ε that the tile's outputs at
+// plane k read is non-zero: corners i ∈ [i0, i0+TX], j ∈ [j0, j0+TY],
+// planes k and k+1.
+__global__ void k_oflags(const double *eoff, long long ncell, int N0, int N1, int N2, int tiles_x, uint8_t *flag) {
+  for (long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x; cell < ncell;
+       cell += (long long)gridDim.x * blockDim.x) {
+    if (eoff[cell] == 0.0 && eoff[ncell + cell] == 0.0 && eoff[2 * ncell + cell] == 0.0) continue;
+    const int i = (int)(cell % N0), j = (int)((cell / N0) % N1), k = (int)(cell / ((long long)N0 * N1));
+    const int tx0 = i / TX, ty0 = j / TY;
+    for (int dx = -1; dx <= 0; ++dx) {
+      const int tx = tx0 + dx;
+      if (tx < 0 || (dx == -1 && i % TX != 0)) continue;
+      for (int dy = -1; dy <= 0; ++dy) {
+        const int ty = ty0 + dy;
+        if (ty < 0 || (dy == -1 && j % TY != 0)) continue;
+        const long long tc = tx + (long long)tiles_x * ty;
+        flag[tc * N2 + k] = 1;
+        if (k > 0) flag[tc * N2 + k - 1] = 1;
+      }
+    }
+  }
+}
+
+int build_oflags(fdfd_handle *h) {
+  if (!h->has_off) return FDFD_OK;
+  const int tiles_x = (h->N[0] + TX - 1) / TX, tiles_y = (h->N[1] + TY - 1) / TY;
+  const size_t nflag = (size_t)tiles_x * tiles_y * h->N[2];
+  if (!h->oflag) {
+    if (cudaMalloc(&h->oflag, nflag) != cudaSuccess) {
+      cudaGetLastError();
+      return set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(oflag) failed");
+    }
+  }
+  int rc = cuda_check(h, cudaMemsetAsync(h->oflag, 0, nflag, h->stream), "memset oflag");
+  if (rc) return rc;
+  k_oflags<<<152 * 4, 256, 0, h->stream>>>(h->eoff64, h->ncell, h->N[0], h->N[1], h->N[2], tiles_x, h->oflag);
+  return cuda_check(h, cudaGetLastError(), "k_oflags");
+}
+
+__global__ void k_to_f32(float *dst, const double *src, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    dst[i] = (float)src[i];
+}
+
+static int ensure_eps_buffers(fdfd_handle *h, bool off) {
+  const size_t n = 3 * (size_t)h->ncell;
+  if (!h->eps64) {
+    if (cudaMalloc(&h->eps64, n * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&h->eps32, n * sizeof(float)) != cudaSuccess) {
+      cudaGetLastError();
+      return set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(eps) failed");
+    }
+  }
+  if (off && !h->eoff64) {
+    if (cudaMalloc(&h->eoff64, n * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&h->eoff32, n * sizeof(float)) != cudaSuccess) {
+      cudaGetLastError();
+      return set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(eps off-diagonal) failed");
+    }
+  }
+  return FDFD_OK;
+}
+
+// Refresh the FP32 copies from the FP64 masters and rebuild the flags.
+int finish_eps(fdfd_handle *h) {
+  const long long n = 3 * h->ncell;
+  k_to_f32<<<152 * 4, 256, 0, h->stream>>>(h->eps32, h->eps64, n);
+  int rc = cuda_check(h, cudaGetLastError(), "k_to_f32");
+  if (rc) return rc;
+  if (h->has_off) {
+    k_to_f32<<<152 * 4, 256, 0, h->stream>>>(h->eoff32, h->eoff64, n);
+    rc = cuda_check(h, cudaGetLastError(), "k_to_f32");
+    if (rc) return rc;
+    rc = build_oflags(h);
+    if (rc) return rc;
+  }
+  return cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
+}
+
+// eps_diag_aos[c + 3 cell], eps_off_aos[p + 3 cell] (or null) → SoA on device
+int upload_eps(fdfd_handle *h, const double *eps_diag_aos, const double *eps_off_aos) {
+  const long long nc = h->ncell;
+  bool off = false;
+  if (eps_off_aos)
+    for (long long i = 0; i < 3 * nc && !off; ++i) off = eps_off_aos[i] != 0.0;
+  int rc = ensure_eps_buffers(h, off);
+  if (rc) return rc;
+  std::vector<double> soa(3 * (size_t)nc);
+  for (long long cell = 0; cell < nc; ++cell)
+    for (int c = 0; c < 3; ++c) soa[c * nc + cell] = eps_diag_aos[c + 3 * cell];
+  rc = cuda_check(h, cudaMemcpy(h->eps64, soa.data(), soa.size() * sizeof(double), cudaMemcpyHostToDevice),
+                  "upload eps");
+  if (rc) return rc;
+  h->has_off = off;
+  if (off) {
+    for (long long cell = 0; cell < nc; ++cell)
+      for (int p = 0; p < 3; ++p) soa[p * nc + cell] = eps_off_aos[p + 3 * cell];
+    rc = cuda_check(h, cudaMemcpy(h->eoff64, soa.data(), soa.size() * sizeof(double), cudaMemcpyHostToDevice),
+                    "upload eps off");
+    if (rc) return rc;
+  }
+  return finish_eps(h);
+}
+
+static int ensure_scratch(fdfd_handle *h, bool c64) {
+  const size_t n = 3 * (size_t)h->ncell;
+  if (!h->vx64) {
+    if (cudaMalloc(&h->vx64, n * sizeof(double2)) != cudaSuccess ||
+        cudaMalloc(&h->vy64, n * sizeof(double2)) != cudaSuccess) {
+      cudaGetLastError();
+      return set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(scratch) failed");
+    }
+  }
+  if (c64 && !h->vx32) {
+    if (cudaMalloc(&h->vx32, n * sizeof(float2)) != cudaSuccess ||
+        cudaMalloc(&h->vy32, n * sizeof(float2)) != cudaSuccess) {
+      cudaGetLastError();
+      return set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(scratch c64) failed");
+    }
+  }
+  return FDFD_OK;
+}
+
+static bool transpose_ok(const fdfd_handle *h) {
+  for (int w = 0; w < 3; ++w)
+    if (h->bloch[w] && (h->e_ikl[w][0] != 1.0 || h->e_ikl[w][1] != 0.0)) return false;
+  return true;
+}
+
+static int matvec_host(fdfd_handle *h, const double *x, double *y, int precision, bool tr) {
+  if (!h || !x || !y) return set_error(h, FDFD_ERR_ARG, "null argument");
+  if (precision != FDFD_C128 && precision != FDFD_C64) return set_error(h, FDFD_ERR_ARG, "bad precision");
+  if (tr && !transpose_ok(h)) return set_error(h, FDFD_ERR_UNSUPPORTED, "transpose with a Bloch phase");
+  int rc = ensure_scratch(h, precision == FDFD_C64);
+  if (rc) return rc;
+  const long long n = 3 * h->ncell;
+  rc = cuda_check(h, cudaMemcpyAsync(h->vx64, x, n * sizeof(double2), cudaMemcpyHostToDevice, h->stream), "H2D x");
+  if (rc) return rc;
+  if (precision == FDFD_C64) {
+    if ((rc = demote(h, h->vx32, h->vx64, n))) return rc;
+    if ((rc = launch_apply_fin<float>(h, h->vx32, h->vy32, EPI_STORE, nullptr, FIN_NONE, nullptr, tr))) return rc;
+    if ((rc = promote(h, h->vy64, h->vy32, n))) return rc;
+  } else {
+    if ((rc = launch_apply_fin<double>(h, h->vx64, h->vy64, EPI_STORE, nullptr, FIN_NONE, nullptr, tr))) return rc;
+  }
+  rc = cuda_check(h, cudaMemcpyAsync(y, h->vy64, n * sizeof(double2), cudaMemcpyDeviceToHost, h->stream), "D2H y");
+  if (rc) return rc;
+  return cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
+}
+
+}  // namespace fdfd
+
+using namespace fdfd;
+
+extern "C" {
+
+const char *fdfd_version(void) { return "fdfd_gb300 0.1 (sm_103a)"; }
+
+const char *fdfd_last_error(const fdfd_handle *h) {
+  if (h) return h->err.c_str();
+  return g_last_error.c_str();
+}
+
+void fdfd_default_opts(fdfd_solve_opts *o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->method = FDFD_BICGSTAB;
+  o->precision = FDFD_PREC_MIXED;
+  o->tol = 1e-6;
+  o->maxit = 200000;
+  o->delta = 0.1;
+  o->x0_given = 0;
+  o->check_every = 50;
+  o->transpose = 0;
+  o->use_graph = 1;
+}
+
+int fdfd_create(const fdfd_desc *d, fdfd_handle **out) {
+  if (!d || !out) return set_error(nullptr, FDFD_ERR_ARG, "null argument");
+  *out = nullptr;
+  for (int w = 0; w < 3; ++w) {
+    if (d->N[w] < 1) return set_error(nullptr, FDFD_ERR_ARG, "N must be >= 1 on every axis");
+    if (!d->sdl_e[w] || !d->sdl_m[w]) return set_error(nullptr, FDFD_ERR_ARG, "null s∆l array");
+    if (d->boundft[w] != FDFD_EE) return set_error(nullptr, FDFD_ERR_UNSUPPORTED, "boundft = HH is not supported");
+    if (d->isbloch[w] != 0 && d->isbloch[w] != 1) return set_error(nullptr, FDFD_ERR_ARG, "isbloch must be 0 or 1");
+    if (!d->isbloch[w] && d->N[w] < 2) return set_error(nullptr, FDFD_ERR_ARG, "N must be >= 2 on a symmetry axis");
+  }
+  if (d->order_cmpfirst != 1) return set_error(nullptr, FDFD_ERR_UNSUPPORTED, "order_cmpfirst = false");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return set_error(nullptr, FDFD_ERR_NO_DEVICE, "no CUDA device");
+  }
+  if (d->device < 0 || d->device >= ndev) return set_error(nullptr, FDFD_ERR_ARG, "bad device ordinal");
+  fdfd_handle *h = new fdfd_handle();
+  h->dev = d->device;
+  int rc;
+  if ((rc = cuda_check(h, cudaSetDevice(h->dev), "cudaSetDevice"))) { delete h; return rc; }
+  if ((rc = cuda_check(h, cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream"))) {
+    delete h;
+    return rc;
+  }
+  cudaEventCreate(&h->ev0);
+  cudaEventCreate(&h->ev1);
+  for (int w = 0; w < 3; ++w) {
+    h->N[w] = d->N[w];
+    h->bloch[w] = d->isbloch[w];
+    h->e_ikl[w][0] = d->e_ikl[w][0];
+    h->e_ikl[w][1] = d->e_ikl[w][1];
+    if (!h->bloch[w]) { h->e_ikl[w][0] = 1.0; h->e_ikl[w][1] = 0.0; }
+  }
+  h->ncell = (long long)h->N[0] * h->N[1] * h->N[2];
+  h->omega[0] = d->omega[0];
+  h->omega[1] = d->omega[1];
+  const cd om(d->omega[0], d->omega[1]);
+  const cd w2 = om * om;
+  h->w2[0] = w2.real();
+  h->w2[1] = w2.imag();
+  // per-axis coefficients, 6 kinds: cm, ce, wm, wp, s∆lₑ, s∆lₘ
+  const int st = h->N[0] + h->N[1] + h->N[2];
+  h->coef_stride = st;
+  h->coef_off[0] = 0;
+  h->coef_off[1] = h->N[0];
+  h->coef_off[2] = h->N[0] + h->N[1];
+  std::vector<double2> c64(6 * (size_t)st);
+  std::vector<float2> c32(6 * (size_t)st);
+  for (int w = 0; w < 3; ++w) {
+    const int N = h->N[w];
+    for (int i = 0; i < N; ++i) {
+      const cd se(d->sdl_e[w][2 * i], d->sdl_e[w][2 * i + 1]);
+      const cd sm(d->sdl_m[w][2 * i], d->sdl_m[w][2 * i + 1]);
+      if (std::abs(se) == 0.0 || std::abs(sm) == 0.0 || !std::isfinite(std::abs(se)) || !std::isfinite(std::abs(sm))) {
+        fdfd_destroy(h);
+        return set_error(nullptr, FDFD_ERR_ARG, "s∆l entries must be finite and non-zero");
+      }
+      const int jm = i > 0 ? i - 1 : (h->bloch[w] ? N - 1 : 0);
+      const cd smm(d->sdl_m[w][2 * jm], d->sdl_m[w][2 * jm + 1]);
+      const cd vals[6] = {1.0 / sm, 1.0 / se, smm / (2.0 * se), sm / (2.0 * se), se, sm};
+      for (int kd = 0; kd < 6; ++kd) {
+        const size_t idx = (size_t)kd * st + h->coef_off[w] + i;
+        c64[idx] = make_double2(vals[kd].real(), vals[kd].imag());
+        c32[idx] = make_float2((float)vals[kd].real(), (float)vals[kd].imag());
+      }
+    }
+  }
+  if (cudaMalloc(&h->coef64, c64.size() * sizeof(double2)) != cudaSuccess ||
+      cudaMalloc(&h->coef32, c32.size() * sizeof(float2)) != cudaSuccess) {
+    cudaGetLastError();
+    fdfd_destroy(h);
+    return set_error(nullptr, FDFD_ERR_NOMEM, "cudaMalloc(coefficients) failed");
+  }
+  cudaMemcpy(h->coef64, c64.data(), c64.size() * sizeof(double2), cudaMemcpyHostToDevice);
+  cudaMemcpy(h->coef32, c32.data(), c32.size() * sizeof(float2), cudaMemcpyHostToDevice);
+  // ε = 1 (vacuum) until set
+  if ((rc = ensure_eps_buffers(h, false))) { fdfd_destroy(h); return rc; }
+  {
+    std::vector<double> ones(3 * (size_t)h->ncell, 1.0);
+    cudaMemcpy(h->eps64, ones.data(), ones.size() * sizeof(double), cudaMemcpyHostToDevice);
+  }
+  if ((rc = finish_eps(h))) { fdfd_destroy(h); return rc; }
+  if ((rc = ensure_red(h, apply_blocks(h)))) { fdfd_destroy(h); return rc; }
+  if ((rc = cuda_check(h, cudaStreamSynchronize(h->stream), "create sync"))) { fdfd_destroy(h); return rc; }
+  *out = h;
+  return FDFD_OK;
+}
+
+void fdfd_destroy(fdfd_handle *h) {
+  if (!h) return;
+  cudaSetDevice(h->dev);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  free_workspace(h);
+  cudaFree(h->coef64);
+  cudaFree(h->coef32);
+  cudaFree(h->eps64);
+  cudaFree(h->eps32);
+  cudaFree(h->eoff64);
+  cudaFree(h->eoff32);
+  cudaFree(h->oflag);
+  cudaFree(h->smask);
+  cudaFree(h->vx64);
+  cudaFree(h->vy64);
+  cudaFree(h->vx32);
+  cudaFree(h->vy32);
+  cudaFree(h->red.part);
+  cudaFree(h->red.count);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+void *fdfd_stream(fdfd_handle *h) { return h ? (void *)h->stream : nullptr; }
+
+int fdfd_sync(fdfd_handle *h) {
+  if (!h) return set_error(nullptr, FDFD_ERR_ARG, "null handle");
+  return cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
+}
+
+int fdfd_set_eps(fdfd_handle *h, const double *eps_diag, const double *eps_off) {
+  if (!h || !eps_diag) return set_error(h, FDFD_ERR_ARG, "null argument");
+  cudaSetDevice(h->dev);
+  return upload_eps(h, eps_diag, eps_off);
+}
+
+int fdfd_set_eps_tensor(fdfd_handle *h, const double *epsarr) {
+  if (!h || !epsarr) return set_error(h, FDFD_ERR_ARG, "null argument");
+  cudaSetDevice(h->dev);
+  const long long nc = h->ncell;
+  // column-major (Nx,Ny,Nz,3,3): element (cell, r, c) at cell + nc*(r + 3c)
+  auto at = [&](long long cell, int r, int c, int part) { return epsarr[2 * (cell + nc * (r + 3 * c)) + part]; };
+  std::vector<double> diag(3 * (size_t)nc), off(3 * (size_t)nc);
+  const int pr[3][2] = {{0, 1}, {1, 2}, {2, 0}};
+  for (long long cell = 0; cell < nc; ++cell) {
+    for (int c = 0; c < 3; ++c) {
+      if (at(cell, c, c, 1) != 0.0) return set_error(h, FDFD_ERR_UNSUPPORTED, "complex ε (lossy material)");
+      diag[c + 3 * cell] = at(cell, c, c, 0);
+    }
+    for (int p = 0; p < 3; ++p) {
+      const double a = at(cell, pr[p][0], pr[p][1], 0), b = at(cell, pr[p][1], pr[p][0], 0);
+      if (at(cell, pr[p][0], pr[p][1], 1) != 0.0 || at(cell, pr[p][1], pr[p][0], 1) != 0.0)
+        return set_error(h, FDFD_ERR_UNSUPPORTED, "complex off-diagonal ε");
+      if (a != b) return set_error(h, FDFD_ERR_UNSUPPORTED, "non-symmetric ε tensor");
+      off[p + 3 * cell] = a;
+    }
+  }
+  return upload_eps(h, diag.data(), off.data());
+}
+
+int fdfd_smooth_objects(fdfd_handle *h, const double *const lprim[3], const fdfd_object *objs, int32_t nobj,
+                        double eps_bg, const fdfd_design *design) {
+  if (!h || !lprim || (nobj > 0 && !objs) || nobj < 0) return set_error(h, FDFD_ERR_ARG, "bad argument");
+  for (int w = 0; w < 3; ++w)
+    if (!lprim[w]) return set_error(h, FDFD_ERR_ARG, "null lprim");
+  cudaSetDevice(h->dev);
+  return smooth_objects_impl(h, lprim, objs, nobj, eps_bg, design);
+}
+
+int fdfd_get_eps(fdfd_handle *h, double *eps_diag, double *eps_off, uint8_t *smask) {
+  if (!h) return set_error(nullptr, FDFD_ERR_ARG, "null handle");
+  cudaSetDevice(h->dev);
+  const long long nc = h->ncell;
+  std::vector<double> soa(3 * (size_t)nc);
+  int rc;
+  if (eps_diag) {
+    if ((rc = cuda_check(h, cudaMemcpy(soa.data(), h->eps64, soa.size() * sizeof(double), cudaMemcpyDeviceToHost),
+                         "D2H eps")))
+      return rc;
+    for (long long cell = 0; cell < nc; ++cell)
+      for (int c = 0; c < 3; ++c) eps_diag[c + 3 * cell] = soa[c * nc + cell];
+  }
+  if (eps_off) {
+    if (h->has_off) {
+      if ((rc = cuda_check(h, cudaMemcpy(soa.data(), h->eoff64, soa.size() * sizeof(double),
+                                         cudaMemcpyDeviceToHost), "D2H eoff")))
+        return rc;
+      for (long long cell = 0; cell < nc; ++cell)
+        for (int p = 0; p < 3; ++p) eps_off[p + 3 * cell] = soa[p * nc + cell];
+    } else {
+      std::memset(eps_off, 0, 3 * (size_t)nc * sizeof(double));
+    }
+  }
+  if (smask) {
+    if (h->smask) {
+      if ((rc = cuda_check(h, cudaMemcpy(smask, h->smask, 4 * (size_t)nc, cudaMemcpyDeviceToHost), "D2H smask")))
+        return rc;
+    } else {
+      std::memset(smask, 0, 4 * (size_t)nc);
+    }
+  }
+  return FDFD_OK;
+}
+
+int fdfd_matvec(fdfd_handle *h, const double *x, double *y, int32_t precision) {
+  if (!h) return set_error(nullptr, FDFD_ERR_ARG, "null handle");
+  cudaSetDevice(h->dev);
+  return matvec_host(h, x, y, precision, false);
+}
+
+int fdfd_matvec_transpose(fdfd_handle *h, const double *x, double *y, int32_t precision) {
+  if (!h) return set_error(nullptr, FDFD_ERR_ARG, "null handle");
+  cudaSetDevice(h->dev);
+  return matvec_host(h, x, y, precision, true);
+}
+
+int fdfd_matvec_dev(fdfd_handle *h, const void *x, void *y, int32_t precision) {
+  if (!h || !x || !y) return set_error(h, FDFD_ERR_ARG, "null argument");
+  cudaSetDevice(h->dev);
+  if (precision == FDFD_C64)
+    return launch_apply_fin<float>(h, (const float2 *)x, (float2 *)y, EPI_STORE, nullptr, FIN_NONE, nullptr, false);
+  if (precision == FDFD_C128)
+    return launch_apply_fin<double>(h, (const double2 *)x, (double2 *)y, EPI_STORE, nullptr, FIN_NONE, nullptr,
+                                    false);
+  return set_error(h, FDFD_ERR_ARG, "bad precision");
+}
+
+static int check_opts(fdfd_handle *h, const fdfd_solve_opts *o) {
+  if (!o) return set_error(h, FDFD_ERR_ARG, "null options");
+  if (o->precision != FDFD_PREC_FP64 && o->precision != FDFD_PREC_MIXED)
+    return set_error(h, FDFD_ERR_ARG, "bad precision");
+  if (o->method != FDFD_BICGSTAB && o->method != FDFD_COCG) return set_error(h, FDFD_ERR_ARG, "bad method");
+  if (!(o->tol > 0.0) || o->maxit < 1) return set_error(h, FDFD_ERR_ARG, "bad tol/maxit");
+  if (o->precision == FDFD_PREC_MIXED && !(o->delta > 0.0 && o->delta < 1.0))
+    return set_error(h, FDFD_ERR_ARG, "delta must be in (0, 1)");
+  if (o->transpose && !transpose_ok(h)) return set_error(h, FDFD_ERR_UNSUPPORTED, "transpose with a Bloch phase");
+  if (o->method == FDFD_COCG && !transpose_ok(h))
+    return set_error(h, FDFD_ERR_UNSUPPORTED, "COCG needs a complex-symmetric operator (no Bloch phase)");
+  return FDFD_OK;
+}
+
+int fdfd_solve_dev(fdfd_handle *h, const void *b, void *x, const fdfd_solve_opts *opts, fdfd_stats *stats) {
+  if (!h || !b || !x) return set_error(h, FDFD_ERR_ARG, "null argument");
+  int rc = check_opts(h, opts);
+  if (rc) return rc;
+  cudaSetDevice(h->dev);
+  return solve_dev_impl(h, (const double2 *)b, (double2 *)x, opts, stats);
+}
+
+int fdfd_solve(fdfd_handle *h, const double *b, double *x, int32_t nrhs, const fdfd_solve_opts *opts,
+               fdfd_stats *stats) {
+  if (!h || !b || !x || nrhs < 1) return set_error(h, FDFD_ERR_ARG, "bad argument");
+  int rc = check_opts(h, opts);
+  if (rc) return rc;
+  cudaSetDevice(h->dev);
+  if ((rc = ensure_scratch(h, false))) return rc;
+  const long long n = 3 * h->ncell;
+  int first_err = FDFD_OK;
+  std::string first_msg;
+  for (int q = 0; q < nrhs; ++q) {
+    const double *bq = b + 2 * n * q;
+    double *xq = x + 2 * n * q;
+    rc = cuda_check(h, cudaMemcpyAsync(h->vx64, bq, n * sizeof(double2), cudaMemcpyHostToDevice, h->stream), "H2D b");
+    if (rc) return rc;
+    if (opts->x0_given) {
+      rc = cuda_check(h, cudaMemcpyAsync(h->vy64, xq, n * sizeof(double2), cudaMemcpyHostToDevice, h->stream),
+                      "H2D x0");
+      if (rc) return rc;
+    }
+    rc = solve_dev_impl(h, h->vx64, h->vy64, opts, stats ? stats + q : nullptr);
+    if (rc && rc != FDFD_ERR_NOT_CONVERGED && rc != FDFD_ERR_BREAKDOWN) return rc;
+    if (rc && first_err == FDFD_OK) {
+      first_err = rc;
+      first_msg = h->err;
+    }
+    int rc2 = cuda_check(h, cudaMemcpyAsync(xq, h->vy64, n * sizeof(double2), cudaMemcpyDeviceToHost, h->stream),
+                         "D2H x");
+    if (rc2) return rc2;
+    if ((rc2 = cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync"))) return rc2;
+  }
+  if (first_err) return set_error(h, first_err, first_msg);
+  return FDFD_OK;
+}
+
+int fdfd_eps_grad(fdfd_handle *h, const double *e, const double *g, double *grad, const fdfd_solve_opts *opts,
+                  fdfd_stats *stats) {
+  (void)e; (void)g; (void)grad; (void)opts; (void)stats;
+  return set_error(h, FDFD_ERR_UNSUPPORTED, "fdfd_eps_grad is not available in this build yet");
+}
+
+}  // extern "C"

@@ -1,0 +1,152 @@
+// Internal declarations shared by the translation units of libfdfd_gb300.
+//
+// Data layout in HBM (per handle):
+//   field vectors   AoS complex, component fastest: v[c + 3*cell],
+//                   cell = i + Nx*(j + Ny*k)  (the reference's order_cmpfirst
+//                   DOF order, model.jl:85, 88-94) — float2 or double2.
+//   eps diagonal    SoA real: eps[c*Ncell + cell] = ε_cc at the E_c sample.
+//   eps off-diag    SoA real: eoff[p*Ncell + cell], p = xy, yz, zx, at the
+//                   E-voxel corner (primal³ point) of the cell.
+//   per-axis coefs  complex, length N[w]:  cm = 1/s∆lₘ (curl E→H), ce = 1/s∆lₑ
+//                   (curl H→E), wm/wp = corner-averaging weights
+//                   s∆lₘ[j-1]/(2 s∆lₑ[j]), s∆lₘ[j]/(2 s∆lₑ[j]).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/fdfd_gb300.h"
+
+namespace fdfd {
+
+// ---------------------------------------------------------------- complex
+template <typename R> struct CT;
+template <> struct CT<float> { using C = float2; };
+template <> struct CT<double> { using C = double2; };
+
+__host__ __device__ __forceinline__ float2 mk(float a, float b) { return make_float2(a, b); }
+__host__ __device__ __forceinline__ double2 mk(double a, double b) { return make_double2(a, b); }
+template <typename C> __host__ __device__ __forceinline__ C cadd(C a, C b) { return mk(a.x + b.x, a.y + b.y); }
+template <typename C> __host__ __device__ __forceinline__ C csub(C a, C b) { return mk(a.x - b.x, a.y - b.y); }
+template <typename C> __host__ __device__ __forceinline__ C cmul(C a, C b) {
+  return mk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+template <typename C, typename R> __host__ __device__ __forceinline__ C cscale(C a, R s) { return mk(a.x * s, a.y * s); }
+// conj(a) * b
+template <typename C> __host__ __device__ __forceinline__ C cdotc(C a, C b) {
+  return mk(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+template <typename C> __host__ __device__ __forceinline__ C czero() { return mk(decltype(C{}.x)(0), decltype(C{}.x)(0)); }
+
+// ---------------------------------------------------------------- tiling
+constexpr int TX = 32;   // tile width (x), one warp
+constexpr int TY = 8;    // tile height (y)
+constexpr int NTHR = TX * TY;
+
+// ---------------------------------------------------------------- operator
+template <typename R>
+struct OpArgs {
+  using C = typename CT<R>::C;
+  int N[3];
+  int bloch[3];
+  long long ncell;
+  const C *cm[3], *ce[3], *wm[3], *wp[3];
+  const R *eps;      // 3*ncell (SoA)
+  const R *eoff;     // 3*ncell (SoA) or nullptr
+  const uint8_t *oflag;  // per (tile, z-plane) flag: off-diagonal present; nullptr = everywhere
+  C w2;              // ω²
+};
+
+// Epilogue of the stencil: what to do with y = A x at each cell.
+enum EpiKind : int {
+  EPI_STORE = 0,        // y = A x
+  EPI_RESID = 1,        // y = b - A x, accumulate ‖y‖²       (aux0 = b)
+  EPI_DOT_AUX = 2,      // y = A x, accumulate conj(aux0)·y     (aux0 = r̂)
+  EPI_DOT_TS = 3,       // y = A x, accumulate conj(y)·x, ‖y‖²  (t = A s)
+};
+
+// Reduction slots used by the fused kernels: each kernel accumulates up to
+// two complex partial sums per block into part[blk*2 + {0,1}] (FP64).
+struct RedBuf {
+  double2 *part;         // >= 2 * max blocks
+  unsigned int *count;   // arrival counter for the last-block finalisation
+};
+
+// Scalars of a Krylov iteration, resident in device memory so that whole
+// batches of iterations run (and replay as a CUDA graph) without host sync.
+struct KScalars {
+  double2 rho, alpha, omega, beta;
+  double2 dot0, dot1;    // raw finalised reductions of the last kernel
+  double rr;             // recursive ‖r‖² (inner precision)
+  double rr_max;         // largest ‖r‖² since the last reliable update
+  double bb;             // ‖b‖²
+  double stop2;          // recursive-residual stop threshold (‖r‖²)
+  double upd2;           // δ²: reliable update when rr < upd2 * rr_max
+  int done;              // 1: later kernels of the batch are no-ops
+  int reason;            // 1 recursive converged, 2 reliable update due, 3 breakdown, 4 nonfinite
+  long long iter;
+};
+
+struct Workspace;  // solver vectors (solver.cu)
+
+}  // namespace fdfd
+
+struct fdfd_handle {
+  int dev = 0;
+  cudaStream_t stream = nullptr;
+  int N[3] = {0, 0, 0};
+  int bloch[3] = {0, 0, 0};
+  long long ncell = 0;
+  double omega[2] = {0, 0};
+  double w2[2] = {0, 0};
+  double e_ikl[3][2];
+  // per-axis coefficients: [kind(4)][axis(3)] contiguous, kind = cm, ce, wm, wp
+  double2 *coef64 = nullptr;
+  float2 *coef32 = nullptr;
+  long long coef_off[3] = {0, 0, 0};
+  int coef_stride = 0;  // = N[0]+N[1]+N[2]
+  double *eps64 = nullptr;
+  float *eps32 = nullptr;
+  double *eoff64 = nullptr;
+  float *eoff32 = nullptr;
+  uint8_t *oflag = nullptr;
+  bool has_off = false;
+  uint8_t *smask = nullptr;  // 4*ncell smoothing mask (from fdfd_smooth_objects)
+  // scratch for host-pointer entry points
+  double2 *vx64 = nullptr, *vy64 = nullptr;
+  float2 *vx32 = nullptr, *vy32 = nullptr;
+  fdfd::RedBuf red{nullptr, nullptr};
+  int red_blocks = 0;
+  fdfd::Workspace *ws = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::string err;
+};
+
+namespace fdfd {
+
+int set_error(fdfd_handle *h, int code, const std::string &msg);
+int cuda_check(fdfd_handle *h, cudaError_t e, const char *what);
+
+template <typename R> OpArgs<R> op_args(const fdfd_handle *h);
+
+// Launch y = A x (or Aᵀ x), with the fused epilogue `epi` and, for reducing
+// epilogues, the finalisation `fin` into `sc` (which also gates the launch:
+// sc->done != 0 turns it into a no-op).  On the handle's stream.
+template <typename R>
+int launch_apply_fin(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R>::C *y, int epi,
+                     const typename CT<R>::C *aux0, int fin, KScalars *sc, bool transpose);
+// number of blocks launch_apply uses (reduction buffer sizing)
+int apply_blocks(const fdfd_handle *h);
+
+// Finalise per-block partials; defined in blas1.cu
+int ensure_red(fdfd_handle *h, int blocks);
+
+void free_workspace(fdfd_handle *h);
+int smooth_objects_impl(fdfd_handle *h, const double *const lprim[3], const fdfd_object *objs, int nobj,
+                        double eps_bg, const fdfd_design *design);
+int upload_eps(fdfd_handle *h, const double *eps_diag_aos, const double *eps_off_aos);
+int build_oflags(fdfd_handle *h);
+
+}  // namespace fdfd

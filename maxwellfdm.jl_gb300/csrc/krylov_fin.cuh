@@ -1,0 +1,170 @@
+// Grid-wide reductions and the scalar recurrences of the Krylov solvers.
+//
+// Every reducing kernel writes two FP64 complex partials per block; the
+// last block to arrive (atomic counter) sums them in block order — so the
+// result is deterministic — and runs the scalar update of the solver step
+// (finalise).  No block ever waits on another: the counter is only read by
+// the block that incremented it last.
+#pragma once
+
+#include "fdfd_internal.cuh"
+
+namespace fdfd {
+
+enum FinMode : int {
+  FIN_NONE = 0,    // store the sums in sc->dot0 / sc->dot1
+  FIN_ALPHA = 1,   // BiCGSTAB: α = ρ / (r̂, v)
+  FIN_OMEGA = 2,   // BiCGSTAB: ω = (t, s) / (t, t)
+  FIN_XR = 3,      // BiCGSTAB: ρ' = (r̂, r), β = ρ'/ρ · α/ω, ‖r‖², stop tests
+  FIN_RESID = 4,   // ‖b − A x‖² into dot0.x (reliable update / final check)
+  FIN_COCG_A = 5,  // COCG: α = ρ / (pᵀ q)
+  FIN_COCG_R = 6,  // COCG: ρ' = rᵀ r, β = ρ'/ρ, ‖r‖², stop tests
+};
+
+__device__ __forceinline__ double2 dcdiv(double2 a, double2 b) {
+  double d = b.x * b.x + b.y * b.y;
+  return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
+__device__ __forceinline__ double2 dcmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ bool dfinite(double2 a) { return isfinite(a.x) && isfinite(a.y); }
+
+__device__ __forceinline__ void stop_tests(KScalars *sc, double rr) {
+  sc->rr = rr;
+  sc->iter += 1;
+  if (rr > sc->rr_max) sc->rr_max = rr;
+  if (!isfinite(rr)) { sc->done = 1; sc->reason = 4; return; }
+  if (rr <= sc->stop2) { sc->done = 1; sc->reason = 1; return; }
+  if (rr <= sc->upd2 * sc->rr_max) { sc->done = 1; sc->reason = 2; return; }
+}
+
+__device__ inline void finalise(int mode, KScalars *sc, double2 d0, double2 d1) {
+  sc->dot0 = d0;
+  sc->dot1 = d1;
+  switch (mode) {
+    case FIN_ALPHA: {
+      if (!dfinite(d0)) { sc->done = 1; sc->reason = 4; break; }
+      if (d0.x == 0.0 && d0.y == 0.0) { sc->done = 1; sc->reason = 3; break; }
+      sc->alpha = dcdiv(sc->rho, d0);
+      break;
+    }
+    case FIN_OMEGA: {
+      if (!dfinite(d0) || !isfinite(d1.x)) { sc->done = 1; sc->reason = 4; break; }
+      sc->omega = d1.x > 0.0 ? make_double2(d0.x / d1.x, d0.y / d1.x) : make_double2(0.0, 0.0);
+      break;
+    }
+    case FIN_XR: {
+      double2 rho_new = d0;
+      double2 om = sc->omega;
+      if (om.x == 0.0 && om.y == 0.0) { stop_tests(sc, d1.x); if (!sc->done) { sc->done = 1; sc->reason = 3; } break; }
+      if (rho_new.x == 0.0 && rho_new.y == 0.0) { stop_tests(sc, d1.x); if (!sc->done) { sc->done = 1; sc->reason = 3; } break; }
+      sc->beta = dcmul(dcdiv(rho_new, sc->rho), dcdiv(sc->alpha, om));
+      sc->rho = rho_new;
+      stop_tests(sc, d1.x);
+      break;
+    }
+    case FIN_COCG_A: {
+      if (!dfinite(d0)) { sc->done = 1; sc->reason = 4; break; }
+      if (d0.x == 0.0 && d0.y == 0.0) { sc->done = 1; sc->reason = 3; break; }
+      sc->alpha = dcdiv(sc->rho, d0);
+      break;
+    }
+    case FIN_COCG_R: {
+      double2 rho_new = d0;
+      if (sc->rho.x == 0.0 && sc->rho.y == 0.0) { sc->done = 1; sc->reason = 3; break; }
+      sc->beta = dcdiv(rho_new, sc->rho);
+      sc->rho = rho_new;
+      stop_tests(sc, d1.x);
+      break;
+    }
+    default:
+      break;
+  }
+}
+
+// Block-level reduction of two complex FP64 values, then the grid-level
+// last-block finalisation.  Must be called by every thread of the block.
+template <int NT>
+__device__ inline void block_reduce_finalise(double2 a0, double2 a1, RedBuf red, int mode, KScalars *sc) {
+  __shared__ double2 wred[NT / 32][2];
+  __shared__ bool last;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a0.x += __shfl_xor_sync(0xffffffffu, a0.x, o);
+    a0.y += __shfl_xor_sync(0xffffffffu, a0.y, o);
+    a1.x += __shfl_xor_sync(0xffffffffu, a1.x, o);
+    a1.y += __shfl_xor_sync(0xffffffffu, a1.y, o);
+  }
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int lane = tid & 31, wid = tid >> 5;
+  if (lane == 0) { wred[wid][0] = a0; wred[wid][1] = a1; }
+  __syncthreads();
+  const unsigned nblk = gridDim.x * gridDim.y * gridDim.z;
+  const unsigned bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+  if (tid == 0) {
+    double2 s0 = make_double2(0, 0), s1 = make_double2(0, 0);
+    for (int w = 0; w < NT / 32; ++w) {
+      s0.x += wred[w][0].x; s0.y += wred[w][0].y;
+      s1.x += wred[w][1].x; s1.y += wred[w][1].y;
+    }
+    red.part[2 * bid] = s0;
+    red.part[2 * bid + 1] = s1;
+    __threadfence();
+    unsigned prev = atomicAdd(red.count, 1u);
+    last = (prev == nblk - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  // last block: deterministic sum of all partials in block order
+  __threadfence();
+  double2 s0 = make_double2(0, 0), s1 = make_double2(0, 0);
+  for (unsigned b = tid; b < nblk; b += NT) {
+    double2 p0 = __ldcg(&red.part[2 * b]);
+    double2 p1 = __ldcg(&red.part[2 * b + 1]);
+    s0.x += p0.x; s0.y += p0.y;
+    s1.x += p1.x; s1.y += p1.y;
+  }
+  // fixed-order tree over the block (deterministic for a fixed launch shape)
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    s0.x += __shfl_xor_sync(0xffffffffu, s0.x, o);
+    s0.y += __shfl_xor_sync(0xffffffffu, s0.y, o);
+    s1.x += __shfl_xor_sync(0xffffffffu, s1.x, o);
+    s1.y += __shfl_xor_sync(0xffffffffu, s1.y, o);
+  }
+  __syncthreads();
+  if (lane == 0) { wred[wid][0] = s0; wred[wid][1] = s1; }
+  __syncthreads();
+  if (tid == 0) {
+    double2 t0 = make_double2(0, 0), t1 = make_double2(0, 0);
+    for (int w = 0; w < NT / 32; ++w) {
+      t0.x += wred[w][0].x; t0.y += wred[w][0].y;
+      t1.x += wred[w][1].x; t1.y += wred[w][1].y;
+    }
+    *red.count = 0u;
+    if (sc) finalise(mode, sc, t0, t1);
+  }
+}
+
+// Per-thread accumulator: FP64 for double kernels; for float kernels a
+// compensated (Neumaier) FP32 sum, widened to FP64 before the block
+// reduction — products and the short per-thread sums stay in FP32, every
+// cross-thread and cross-block addition is FP64.
+template <typename R> struct Acc;
+template <> struct Acc<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double v) { s += v; }
+  __device__ __forceinline__ double get() const { return s; }
+};
+template <> struct Acc<float> {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float v) {
+    float t = s + v;
+    c += (fabsf(s) >= fabsf(v)) ? ((s - t) + v) : ((v - t) + s);
+    s = t;
+  }
+  __device__ __forceinline__ double get() const { return (double)s + (double)c; }
+};
+
+}  // namespace fdfd

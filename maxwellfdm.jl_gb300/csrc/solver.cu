@@ -1,0 +1,369 @@
+// Krylov solvers for A x = b (the reference leaves the solve to the user's
+// A\b on the assembled SparseMatrixCSC, src/model/model.jl:222-233).
+//
+// Two precisions share one driver:
+//   FDFD_PREC_FP64   plain complex128 iteration (the comparison baseline);
+//   FDFD_PREC_MIXED  complex64 operator and Krylov vectors, FP64 reductions,
+//                    and reliable updates: whenever the recursive residual
+//                    has dropped by δ since the last update, the complex64
+//                    correction is folded into the FP64 solution x64 and the
+//                    residual is recomputed in FP64, r = b − A·x64, then
+//                    rounded back — the Krylov space is kept (no restart).
+// Convergence is always decided on the true FP64 residual ‖b − A x64‖/‖b‖.
+//
+// The scalars of the recurrences live on the device (KScalars); a batch of
+// `check_every` iterations is one CUDA graph replay with no host sync;
+// kernels become no-ops once a stop condition is reached inside a batch.
+#include <cstring>
+#include <vector>
+
+#include "krylov_fin.cuh"
+
+namespace fdfd {
+
+template <typename R>
+int bicg_p(fdfd_handle *, const typename CT<R>::C *, typename CT<R>::C *, const typename CT<R>::C *, long long,
+           const KScalars *);
+template <typename R>
+int bicg_s(fdfd_handle *, const typename CT<R>::C *, const typename CT<R>::C *, typename CT<R>::C *, long long,
+           const KScalars *);
+template <typename R>
+int bicg_xr(fdfd_handle *, typename CT<R>::C *, const typename CT<R>::C *, const typename CT<R>::C *,
+            const typename CT<R>::C *, typename CT<R>::C *, const typename CT<R>::C *, long long, KScalars *);
+template <typename R>
+int cocg_xr(fdfd_handle *, typename CT<R>::C *, const typename CT<R>::C *, const typename CT<R>::C *,
+            typename CT<R>::C *, const typename CT<R>::C *, long long, KScalars *);
+template <typename R>
+int cocg_p(fdfd_handle *, const typename CT<R>::C *, typename CT<R>::C *, long long, const KScalars *);
+template <typename R>
+int dot(fdfd_handle *, const typename CT<R>::C *, const typename CT<R>::C *, long long, KScalars *);
+template <typename R>
+int dot_u(fdfd_handle *, const typename CT<R>::C *, const typename CT<R>::C *, const typename CT<R>::C *, long long,
+          int, KScalars *);
+template <typename R>
+int copy(fdfd_handle *, typename CT<R>::C *, const typename CT<R>::C *, long long);
+int accum(fdfd_handle *, double2 *, float2 *, long long);
+int accum64(fdfd_handle *, double2 *, double2 *, long long);
+int demote(fdfd_handle *, float2 *, const double2 *, long long);
+int promote(fdfd_handle *, double2 *, const float2 *, long long);
+int build_weights(fdfd_handle *h, double2 *w64, float2 *w32);
+
+#define TRY(x)              \
+  do {                      \
+    int _rc = (x);          \
+    if (_rc) return _rc;    \
+  } while (0)
+
+struct Workspace {
+  long long n = 0;
+  double2 *x64 = nullptr, *r64 = nullptr;
+  float2 *f[7] = {nullptr};
+  double2 *d[7] = {nullptr};
+  double2 *w64 = nullptr;
+  float2 *w32 = nullptr;
+  KScalars *sc = nullptr, *scu = nullptr;
+  KScalars *host = nullptr;  // pinned mirror
+  cudaGraphExec_t gexec[2][2][2] = {};  // [precision][method][transpose]
+  int gbatch[2][2][2] = {};
+};
+
+void free_workspace(fdfd_handle *h) {
+  Workspace *ws = h->ws;
+  if (!ws) return;
+  cudaFree(ws->x64);
+  cudaFree(ws->r64);
+  for (int i = 0; i < 7; ++i) {
+    cudaFree(ws->f[i]);
+    cudaFree(ws->d[i]);
+  }
+  cudaFree(ws->w64);
+  cudaFree(ws->w32);
+  cudaFree(ws->sc);
+  cudaFree(ws->scu);
+  if (ws->host) cudaFreeHost(ws->host);
+  for (auto &a : ws->gexec)
+    for (auto &b : a)
+      for (auto &g : b)
+        if (g) cudaGraphExecDestroy(g);
+  delete ws;
+  h->ws = nullptr;
+}
+
+static int alloc(fdfd_handle *h, void **p, size_t bytes, const char *what) {
+  if (*p) return FDFD_OK;
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return set_error(h, FDFD_ERR_NOMEM, std::string("cudaMalloc failed for ") + what);
+  }
+  return FDFD_OK;
+}
+
+static int ensure_ws(fdfd_handle *h, bool mixed, int method) {
+  if (!h->ws) {
+    h->ws = new Workspace();
+    h->ws->n = 3 * h->ncell;
+  }
+  Workspace *ws = h->ws;
+  const size_t n = (size_t)ws->n;
+  TRY(alloc(h, (void **)&ws->x64, n * sizeof(double2), "x64"));
+  TRY(alloc(h, (void **)&ws->r64, n * sizeof(double2), "r64"));
+  const int nv = (method == FDFD_COCG) ? 4 : 7;
+  for (int i = 0; i < nv; ++i) {
+    if (mixed) TRY(alloc(h, (void **)&ws->f[i], n * sizeof(float2), "inner vector (c64)"));
+    else TRY(alloc(h, (void **)&ws->d[i], n * sizeof(double2), "inner vector (c128)"));
+  }
+  if (method == FDFD_COCG) {
+    if (mixed) TRY(alloc(h, (void **)&ws->w32, n * sizeof(float2), "weights"));
+    else TRY(alloc(h, (void **)&ws->w64, n * sizeof(double2), "weights"));
+    TRY(build_weights(h, mixed ? nullptr : ws->w64, mixed ? ws->w32 : nullptr));
+  }
+  TRY(alloc(h, (void **)&ws->sc, sizeof(KScalars), "scalars"));
+  TRY(alloc(h, (void **)&ws->scu, sizeof(KScalars), "scalars"));
+  if (!ws->host) {
+    if (cudaHostAlloc((void **)&ws->host, 2 * sizeof(KScalars), cudaHostAllocDefault) != cudaSuccess) {
+      cudaGetLastError();
+      return set_error(h, FDFD_ERR_NOMEM, "cudaHostAlloc(scalars) failed");
+    }
+    std::memset(ws->host, 0, 2 * sizeof(KScalars));
+    TRY(cuda_check(h, cudaMemcpyAsync(ws->scu, ws->host + 1, sizeof(KScalars), cudaMemcpyHostToDevice, h->stream),
+                   "init scu"));
+  }
+  return FDFD_OK;
+}
+
+template <typename R> static typename CT<R>::C *vec(Workspace *ws, int i);
+template <> float2 *vec<float>(Workspace *ws, int i) { return ws->f[i]; }
+template <> double2 *vec<double>(Workspace *ws, int i) { return ws->d[i]; }
+template <typename R> static typename CT<R>::C *wvec(Workspace *ws);
+template <> float2 *wvec<float>(Workspace *ws) { return ws->w32; }
+template <> double2 *wvec<double>(Workspace *ws) { return ws->w64; }
+
+static int read_scalars(fdfd_handle *h, const KScalars *dev, KScalars *host) {
+  TRY(cuda_check(h, cudaMemcpyAsync(host, dev, sizeof(KScalars), cudaMemcpyDeviceToHost, h->stream), "read scalars"));
+  return cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
+}
+static int write_scalars(fdfd_handle *h, KScalars *dev, const KScalars *host) {
+  TRY(cuda_check(h, cudaMemcpyAsync(dev, host, sizeof(KScalars), cudaMemcpyHostToDevice, h->stream),
+                 "write scalars"));
+  // the pinned source must stay unchanged until the copy has run
+  return cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
+}
+
+// r64 = b − A x64 (FP64), returns ‖r64‖² on the host
+static int true_residual(fdfd_handle *h, const double2 *b, bool tr, double *rr) {
+  Workspace *ws = h->ws;
+  TRY(launch_apply_fin<double>(h, ws->x64, ws->r64, EPI_RESID, b, FIN_NONE, ws->scu, tr));
+  TRY(read_scalars(h, ws->scu, ws->host + 1));
+  *rr = ws->host[1].dot0.x;
+  return FDFD_OK;
+}
+
+// One BiCGSTAB iteration (5 kernels, 2 operator applications).
+template <typename R>
+static int bicg_iter(fdfd_handle *h, Workspace *ws, bool tr) {
+  using C = typename CT<R>::C;
+  const long long n = ws->n;
+  C *xi = vec<R>(ws, 0), *r = vec<R>(ws, 1), *rh = vec<R>(ws, 2), *p = vec<R>(ws, 3), *v = vec<R>(ws, 4),
+    *s = vec<R>(ws, 5), *t = vec<R>(ws, 6);
+  TRY(bicg_p<R>(h, r, p, v, n, ws->sc));
+  TRY(launch_apply_fin<R>(h, p, v, EPI_DOT_AUX, rh, FIN_ALPHA, ws->sc, tr));
+  TRY(bicg_s<R>(h, r, v, s, n, ws->sc));
+  TRY(launch_apply_fin<R>(h, s, t, EPI_DOT_TS, nullptr, FIN_OMEGA, ws->sc, tr));
+  TRY(bicg_xr<R>(h, xi, p, s, t, r, rh, n, ws->sc));
+  return FDFD_OK;
+}
+
+// One COCG iteration on the S-symmetric operator (1 application):
+//   q = A p ; α = ρ/(pᵀ S q) ; x += α p ; r −= α q ; ρ' = rᵀ S r ; β = ρ'/ρ ; p = r + β p
+template <typename R>
+static int cocg_iter(fdfd_handle *h, Workspace *ws, bool tr) {
+  using C = typename CT<R>::C;
+  const long long n = ws->n;
+  C *xi = vec<R>(ws, 0), *r = vec<R>(ws, 1), *p = vec<R>(ws, 2), *q = vec<R>(ws, 3);
+  TRY(launch_apply_fin<R>(h, p, q, EPI_STORE, nullptr, FIN_NONE, ws->sc, tr));
+  TRY(dot_u<R>(h, p, q, wvec<R>(ws), n, FIN_COCG_A, ws->sc));
+  TRY(cocg_xr<R>(h, xi, p, q, r, wvec<R>(ws), n, ws->sc));
+  TRY(cocg_p<R>(h, r, p, n, ws->sc));
+  return FDFD_OK;
+}
+
+template <typename R>
+static int run_batch(fdfd_handle *h, Workspace *ws, int method, bool tr, int batch, bool use_graph) {
+  const int pi = sizeof(R) == 4 ? 1 : 0;
+  const int mi = method == FDFD_COCG ? 1 : 0;
+  const int ti = tr ? 1 : 0;
+  auto body = [&]() -> int {
+    for (int i = 0; i < batch; ++i) {
+      if (method == FDFD_COCG) TRY(cocg_iter<R>(h, ws, tr));
+      else TRY(bicg_iter<R>(h, ws, tr));
+    }
+    return FDFD_OK;
+  };
+  if (!use_graph) return body();
+  cudaGraphExec_t &ge = ws->gexec[pi][mi][ti];
+  if (ge && ws->gbatch[pi][mi][ti] != batch) {
+    cudaGraphExecDestroy(ge);
+    ge = nullptr;
+  }
+  if (!ge) {
+    // make sure lazily-sized buffers exist before capture
+    TRY(ensure_red(h, apply_blocks(h)));
+    cudaGraph_t g;
+    TRY(cuda_check(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture"));
+    int rc = body();
+    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    if (rc) return rc;
+    TRY(cuda_check(h, e, "end capture"));
+    e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    TRY(cuda_check(h, e, "graph instantiate"));
+    ws->gbatch[pi][mi][ti] = batch;
+  }
+  return cuda_check(h, cudaGraphLaunch(ge, h->stream), "graph launch");
+}
+
+// (Re)initialise the inner iteration from the FP64 residual r64.
+template <typename R>
+static int init_inner(fdfd_handle *h, Workspace *ws, int method, double rr, KScalars *hs) {
+  using C = typename CT<R>::C;
+  const long long n = ws->n;
+  const size_t bytes = (size_t)n * sizeof(C);
+  C *r = vec<R>(ws, 1);
+  if constexpr (sizeof(R) == 4) TRY(demote(h, r, ws->r64, n));
+  else TRY(copy<double>(h, r, ws->r64, n));
+  TRY(cuda_check(h, cudaMemsetAsync(vec<R>(ws, 0), 0, bytes, h->stream), "memset x"));
+  if (method == FDFD_COCG) {
+    // p = r ; ρ = rᵀ S r
+    TRY(copy<R>(h, vec<R>(ws, 2), r, n));
+    TRY(dot_u<R>(h, r, r, wvec<R>(ws), n, FIN_NONE, ws->scu));
+    KScalars tmp;
+    TRY(read_scalars(h, ws->scu, &tmp));
+    hs->rho = tmp.dot0;
+  } else {
+    TRY(copy<R>(h, vec<R>(ws, 2), r, n));  // r̂ = r₀
+    TRY(cuda_check(h, cudaMemsetAsync(vec<R>(ws, 3), 0, bytes, h->stream), "memset p"));
+    TRY(cuda_check(h, cudaMemsetAsync(vec<R>(ws, 4), 0, bytes, h->stream), "memset v"));
+    hs->rho = make_double2(rr, 0.0);
+  }
+  hs->alpha = make_double2(1.0, 0.0);
+  hs->omega = make_double2(1.0, 0.0);
+  hs->beta = make_double2(0.0, 0.0);
+  hs->rr = rr;
+  hs->rr_max = rr;
+  hs->done = 0;
+  hs->reason = 0;
+  return FDFD_OK;
+}
+
+template <typename R>
+static int solve_impl(fdfd_handle *h, const double2 *b, double2 *x, const fdfd_solve_opts &o, fdfd_stats &st) {
+  const bool mixed = sizeof(R) == 4;
+  const bool tr = o.transpose != 0;
+  TRY(ensure_ws(h, mixed, o.method));
+  Workspace *ws = h->ws;
+  const long long n = ws->n;
+  TRY(cuda_check(h, cudaEventRecord(h->ev0, h->stream), "event"));
+  if (o.x0_given) TRY(cuda_check(h, cudaMemcpyAsync(ws->x64, x, n * sizeof(double2), cudaMemcpyDeviceToDevice,
+                                                    h->stream), "copy x0"));
+  else TRY(cuda_check(h, cudaMemsetAsync(ws->x64, 0, n * sizeof(double2), h->stream), "memset x64"));
+  // ‖b‖²
+  TRY(dot<double>(h, b, b, n, ws->scu));
+  KScalars tmp;
+  TRY(read_scalars(h, ws->scu, &tmp));
+  const double bb = tmp.dot1.x;
+  st = fdfd_stats{};
+  if (!(bb > 0.0)) {
+    TRY(cuda_check(h, cudaMemsetAsync(x, 0, n * sizeof(double2), h->stream), "zero x"));
+    st.status = FDFD_OK;
+    return FDFD_OK;
+  }
+  const double tol2 = o.tol * o.tol * bb;
+  double rr;
+  TRY(true_residual(h, b, tr, &rr));
+  st.matvecs = 1;
+  KScalars &hs = ws->host[0];
+  std::memset(&hs, 0, sizeof(KScalars));
+  hs.bb = bb;
+  // recursive-residual target a little below the true target; mixed also
+  // stops every δ-drop for a reliable update
+  hs.stop2 = tol2 * 0.25;
+  hs.upd2 = mixed ? o.delta * o.delta : 0.0;
+  int status = FDFD_ERR_NOT_CONVERGED;
+  int restarts = 0;
+  long long iters = 0;
+  if (rr <= tol2) {
+    status = FDFD_OK;
+  } else {
+    TRY(init_inner<R>(h, ws, o.method, rr, &hs));
+    TRY(write_scalars(h, ws->sc, &hs));
+    const int batch = o.check_every > 0 ? o.check_every : 50;
+    const int mv_per_it = o.method == FDFD_COCG ? 1 : 2;
+    while (true) {
+      TRY(run_batch<R>(h, ws, o.method, tr, batch, o.use_graph != 0));
+      TRY(read_scalars(h, ws->sc, &hs));
+      iters = hs.iter;
+      if (hs.done) {
+        if (hs.reason == 4) { status = FDFD_ERR_NONFINITE; break; }
+        // fold the correction into x64 and recompute the true residual
+        if constexpr (sizeof(R) == 4) TRY(accum(h, ws->x64, vec<R>(ws, 0), n));
+        else TRY(accum64(h, ws->x64, vec<R>(ws, 0), n));
+        TRY(true_residual(h, b, tr, &rr));
+        st.matvecs += 1;
+        st.refinements += 1;
+        if (rr <= tol2) { status = FDFD_OK; break; }
+        if (hs.reason == 3) {
+          if (++restarts > 50) { status = FDFD_ERR_BREAKDOWN; break; }
+          const long long it_keep = hs.iter;
+          TRY(init_inner<R>(h, ws, o.method, rr, &hs));
+          hs.iter = it_keep;
+        } else {
+          // reliable update: replace the recursive residual, keep the Krylov state
+          using C = typename CT<R>::C;
+          C *r = vec<R>(ws, 1);
+          if constexpr (sizeof(R) == 4) TRY(demote(h, r, ws->r64, n));
+          else TRY(copy<double>(h, r, ws->r64, n));
+          hs.rr = rr;
+          hs.rr_max = rr;
+          hs.done = 0;
+          hs.reason = 0;
+        }
+        TRY(write_scalars(h, ws->sc, &hs));
+      }
+      if (iters >= o.maxit) {
+        // fold what we have and report
+        if constexpr (sizeof(R) == 4) TRY(accum(h, ws->x64, vec<R>(ws, 0), n));
+        else TRY(accum64(h, ws->x64, vec<R>(ws, 0), n));
+        TRY(true_residual(h, b, tr, &rr));
+        st.matvecs += 1;
+        status = rr <= tol2 ? FDFD_OK : FDFD_ERR_NOT_CONVERGED;
+        break;
+      }
+    }
+    st.matvecs += iters * mv_per_it;
+  }
+  TRY(cuda_check(h, cudaMemcpyAsync(x, ws->x64, n * sizeof(double2), cudaMemcpyDeviceToDevice, h->stream),
+                 "copy x"));
+  TRY(cuda_check(h, cudaEventRecord(h->ev1, h->stream), "event"));
+  TRY(cuda_check(h, cudaEventSynchronize(h->ev1), "event sync"));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+  st.iterations = iters;
+  st.relres = std::sqrt(rr / bb);
+  st.time_ms = ms;
+  st.status = status;
+  if (status == FDFD_ERR_NOT_CONVERGED)
+    return set_error(h, status, "solver reached maxit before the tolerance");
+  if (status == FDFD_ERR_BREAKDOWN) return set_error(h, status, "Krylov breakdown persisted after restarts");
+  if (status == FDFD_ERR_NONFINITE) return set_error(h, status, "non-finite value in the iteration");
+  return FDFD_OK;
+}
+
+int solve_dev_impl(fdfd_handle *h, const double2 *b, double2 *x, const fdfd_solve_opts *o, fdfd_stats *st) {
+  fdfd_stats tmp;
+  fdfd_stats &s = st ? *st : tmp;
+  if (o->precision == FDFD_PREC_MIXED) return solve_impl<float>(h, b, x, *o, s);
+  return solve_impl<double>(h, b, x, *o, s);
+}
+
+}  // namespace fdfd

@@ -1,0 +1,210 @@
+"""GPU FDFD operator: the drop-in for the reference's assembled A.
+
+The reference returns ``A = Cₘ·(Pμ \\ Cₑ) − ω²·Pε`` as a
+``SparseMatrixCSC{ComplexF64}`` (create_A, src/model/model.jl:238-259) and
+the caller applies ``A*x`` / ``mul!(y, A, x)`` or solves ``A\\b``.
+``FDFDOperator`` exposes the same operations — ``A @ x``, ``A.T @ x``,
+``A.solve(b)`` — executed matrix-free by libfdfd_gb300 on one GPU.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, dptr
+
+
+class FDFDOperator:
+    """Matrix-free A on the GPU (complex128 semantics, DOF order c + 3·cell)."""
+
+    def __init__(self, N, omega, sdl_e, sdl_m, isbloch=(False, False, False), e_ikl=(1, 1, 1), device=0):
+        lib = _lib.load()
+        self.N = tuple(int(n) for n in N)
+        self.ncell = self.N[0] * self.N[1] * self.N[2]
+        self.n = 3 * self.ncell
+        self.omega = complex(omega)
+        d = _lib.fdfd_desc()
+        self._keep = []
+        for w in range(3):
+            d.N[w] = self.N[w]
+            d.isbloch[w] = int(bool(isbloch[w]))
+            d.boundft[w] = _lib.FDFD_EE
+            ph = complex(e_ikl[w])
+            d.e_ikl[w][0], d.e_ikl[w][1] = ph.real, ph.imag
+            se = np.ascontiguousarray(sdl_e[w], dtype=np.complex128)
+            sm = np.ascontiguousarray(sdl_m[w], dtype=np.complex128)
+            if se.shape != (self.N[w],) or sm.shape != (self.N[w],):
+                raise ValueError("s∆l arrays must have N[w] entries")
+            self._keep += [se, sm]
+            d.sdl_e[w] = dptr(se)
+            d.sdl_m[w] = dptr(sm)
+        d.order_cmpfirst = 1
+        d.device = int(device)
+        d.omega[0], d.omega[1] = self.omega.real, self.omega.imag
+        h = C.c_void_p()
+        check(lib.fdfd_create(C.byref(d), C.byref(h)))
+        self._h = h
+        self._lib = lib
+        self._keep = None
+
+    # ---------------------------------------------------------------- basics
+    @property
+    def shape(self):
+        return (self.n, self.n)
+
+    dtype = np.complex128
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.fdfd_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        check(rc, self._h)
+
+    @property
+    def stream(self):
+        return self._lib.fdfd_stream(self._h)
+
+    def sync(self):
+        self._check(self._lib.fdfd_sync(self._h))
+
+    # ---------------------------------------------------------------- material
+    def set_eps(self, eps_diag, eps_off=None):
+        """eps_diag, eps_off: (Nx,Ny,Nz,3) real arrays (ε_cc at E_c; ε_xy, ε_yz,
+        ε_zx at the cell's corner)."""
+        ed = _cell_aos(eps_diag, self.N, np.float64)
+        eo = None if eps_off is None else _cell_aos(eps_off, self.N, np.float64)
+        self._check(self._lib.fdfd_set_eps(self._h, dptr(ed), None if eo is None else dptr(eo)))
+
+    def set_eps_tensor(self, epsarr):
+        """epsarr: the reference's εarr, (Nx,Ny,Nz,3,3) complex indexed
+        [i,j,k,r,c] (stored here in Julia's column-major order)."""
+        e = np.asarray(epsarr, dtype=np.complex128)
+        if e.shape != self.N + (3, 3):
+            raise ValueError(f"εarr must have shape {self.N + (3, 3)}")
+        jl = np.ascontiguousarray(np.transpose(e, (4, 3, 2, 1, 0)))  # column-major bytes
+        self._check(self._lib.fdfd_set_eps_tensor(self._h, dptr(jl)))
+
+    def smooth_objects(self, lprim, objects, eps_bg=1.0, design=None):
+        """On-device assignment + Kottke smoothing of sphere/box objects."""
+        arrs = [np.ascontiguousarray(l, dtype=np.float64) for l in lprim]
+        lp = (_lib._dp * 3)(*[dptr(a) for a in arrs])
+        objs = (_lib.fdfd_object * max(1, len(objects)))()
+        for q, o in enumerate(objects):
+            objs[q] = o.to_c()
+        dptr_ = None
+        keep = None
+        if design is not None:
+            dd = _lib.fdfd_design()
+            for a in range(3):
+                dd.lo[a], dd.hi[a] = design.lo[a], design.hi[a]
+            keep = np.ascontiguousarray(np.transpose(np.asarray(design.eps, np.float64), (2, 1, 0)))
+            dd.eps_cells = dptr(keep)
+            dptr_ = C.pointer(dd)
+        self._check(self._lib.fdfd_smooth_objects(self._h, lp, objs, len(objects), float(eps_bg), dptr_))
+
+    def get_eps(self):
+        """Returns (eps_diag, eps_off, smask) as (Nx,Ny,Nz,3|4) arrays."""
+        ed = np.zeros(self.n)
+        eo = np.zeros(self.n)
+        sm = np.zeros(4 * self.ncell, dtype=np.uint8)
+        self._check(self._lib.fdfd_get_eps(self._h, dptr(ed), dptr(eo), sm.ctypes.data_as(C.POINTER(C.c_uint8))))
+        return (_aos_cell(ed, self.N, 3), _aos_cell(eo, self.N, 3), _aos_cell(sm, self.N, 4))
+
+    # ---------------------------------------------------------------- apply
+    def matvec(self, x, precision="c128"):
+        x = np.ascontiguousarray(x, dtype=np.complex128).reshape(-1)
+        if x.size != self.n:
+            raise ValueError("x has the wrong length")
+        y = np.empty_like(x)
+        self._check(self._lib.fdfd_matvec(self._h, dptr(x), dptr(y), _prec(precision)))
+        return y
+
+    def rmatvec_transpose(self, x, precision="c128"):
+        x = np.ascontiguousarray(x, dtype=np.complex128).reshape(-1)
+        y = np.empty_like(x)
+        self._check(self._lib.fdfd_matvec_transpose(self._h, dptr(x), dptr(y), _prec(precision)))
+        return y
+
+    def __matmul__(self, x):
+        return self.matvec(x)
+
+    @property
+    def T(self):
+        return _Transposed(self)
+
+    def matvec_dev(self, x_ptr, y_ptr, precision="c64"):
+        """y = A x on device pointers (float2 for c64, double2 for c128), asynchronous on the handle's stream."""
+        self._check(self._lib.fdfd_matvec_dev(self._h, C.c_void_p(x_ptr), C.c_void_p(y_ptr), _prec(precision)))
+
+    # ---------------------------------------------------------------- solve
+    def solve(self, b, tol=1e-6, precision="mixed", method="bicgstab", maxit=200000, x0=None, delta=0.1,
+              check_every=50, transpose=False, use_graph=True):
+        """x = A \\ b to a true relative residual ``tol``.  b may hold several
+        right-hand sides as rows of a 2D array.  Returns (x, [stats])."""
+        b = np.ascontiguousarray(b, dtype=np.complex128)
+        nrhs = 1 if b.ndim == 1 else b.shape[0]
+        b2 = b.reshape(nrhs, -1)
+        if b2.shape[1] != self.n:
+            raise ValueError("b has the wrong length")
+        x = np.zeros_like(b2) if x0 is None else np.ascontiguousarray(x0, np.complex128).reshape(nrhs, -1).copy()
+        o = self._opts(tol, precision, method, maxit, x0 is not None, delta, check_every, transpose, use_graph)
+        st = (_lib.fdfd_stats * nrhs)()
+        rc = self._lib.fdfd_solve(self._h, dptr(b2), dptr(x), nrhs, C.byref(o), st)
+        stats = [s.as_dict() for s in st]
+        if rc != _lib.FDFD_OK:
+            err = _lib.FDFDError(rc, (self._lib.fdfd_last_error(self._h) or b"").decode())
+            err.stats = stats
+            err.x = x.reshape(b.shape)
+            raise err
+        return x.reshape(b.shape), stats
+
+    def solve_dev(self, b_ptr, x_ptr, **kw):
+        """Solve with complex128 device buffers (already resident in HBM)."""
+        o = self._opts(kw.get("tol", 1e-6), kw.get("precision", "mixed"), kw.get("method", "bicgstab"),
+                       kw.get("maxit", 200000), kw.get("x0_given", False), kw.get("delta", 0.1),
+                       kw.get("check_every", 50), kw.get("transpose", False), kw.get("use_graph", True))
+        st = _lib.fdfd_stats()
+        self._check(self._lib.fdfd_solve_dev(self._h, C.c_void_p(b_ptr), C.c_void_p(x_ptr), C.byref(o),
+                                             C.byref(st)))
+        return st.as_dict()
+
+    def _opts(self, tol, precision, method, maxit, x0_given, delta, check_every, transpose, use_graph):
+        return _lib.default_opts(
+            tol=float(tol), precision=_lib.FDFD_PREC_MIXED if precision == "mixed" else _lib.FDFD_PREC_FP64,
+            method=_lib.FDFD_COCG if method == "cocg" else _lib.FDFD_BICGSTAB, maxit=int(maxit),
+            x0_given=int(bool(x0_given)), delta=float(delta), check_every=int(check_every),
+            transpose=int(bool(transpose)), use_graph=int(bool(use_graph)))
+
+
+class _Transposed:
+    def __init__(self, A):
+        self.A = A
+
+    def __matmul__(self, x):
+        return self.A.rmatvec_transpose(x)
+
+
+def _prec(p):
+    if p in ("c128", "fp64", _lib.FDFD_C128):
+        return _lib.FDFD_C128
+    if p in ("c64", "fp32", _lib.FDFD_C64):
+        return _lib.FDFD_C64
+    raise ValueError(f"bad precision {p}")
+
+
+def _cell_aos(a, N, dtype):
+    """(Nx,Ny,Nz,m) → flat [c + m·(i + Nx(j + Ny k))]."""
+    a = np.asarray(a, dtype=dtype)
+    return np.ascontiguousarray(np.transpose(a, (2, 1, 0, 3))).reshape(-1)
+
+
+def _aos_cell(v, N, m):
+    return np.transpose(v.reshape(N[2], N[1], N[0], m), (2, 1, 0, 3))

@@ -1,0 +1,151 @@
+"""GPU operator parity: y = A x from libfdfd_gb300 against the oracle's
+assembled sparse A (the reference's create_A composition,
+src/model/model.jl:248-250), on seeded inputs.
+
+Tolerances: complex128 path ≤ 1e-12 relative (2-norm over the vector);
+complex64 path ≤ 1e-5 relative.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+TOL32 = 1e-5
+
+
+def _rand(n, seed):
+    rng = np.random.default_rng(seed)
+    return rng.standard_normal(n) + 1j * rng.standard_normal(n)
+
+
+def _nonuniform(N, seed):
+    rng = np.random.default_rng(seed)
+    return tuple(np.concatenate([[0.0], np.cumsum(rng.uniform(0.6, 1.4, n))]) for n in N)
+
+
+def _case(O, kind):
+    if kind == "vacuum8":
+        g = O.uniform_grid((8, 8, 8))
+        return O.System(g, 2 * np.pi / 5, ((2, 2, 2), (2, 2, 2))), {}
+    if kind == "spheres_odd":
+        g = O.Grid(_nonuniform((13, 10, 9), 1), (False, False, False))
+        objs = [O.Sphere((6.1, 4.8, 4.4), 2.7, 12.25), O.Sphere((9.5, 6.0, 3.0), 1.6, 2.25)]
+        return O.System(g, 2 * np.pi / 7, ((3, 2, 1), (1, 2, 3)), objs), {}
+    if kind == "ragged":
+        g = O.uniform_grid((37, 11, 5))
+        objs = [O.Box((10.3, 2.2, 1.1), (25.7, 8.6, 3.9), 4.0)]
+        return O.System(g, 2 * np.pi / 9, ((4, 0, 0), (3, 2, 1)), objs), {}
+    if kind == "chunks":
+        g = O.uniform_grid((40, 24, 70))
+        objs = [O.Sphere((20.0, 12.0, 30.0), 6.3, 12.25), O.Sphere((12.0, 8.0, 50.0), 4.1, 2.25)]
+        return O.System(g, 2 * np.pi / 10, ((5, 5, 5), (5, 5, 5)), objs), {}
+    if kind == "bloch0":
+        g = O.uniform_grid((9, 7, 6), isbloch=(True, True, True))
+        objs = [O.Sphere((4.4, 3.1, 2.9), 2.2, 6.0)]
+        return O.System(g, 2 * np.pi / 5, ((0, 0, 0), (0, 0, 0)), objs), {}
+    if kind == "blochk":
+        g = O.uniform_grid((10, 8, 6), isbloch=(True, False, True))
+        objs = [O.Sphere((5.2, 4.1, 3.0), 2.0, 6.0)]
+        k = (0.37, 0.0, -0.21)
+        return O.System(g, 2 * np.pi / 5, ((0, 2, 0), (0, 2, 0)), objs, kbloch=k), {"kbloch": k}
+    raise KeyError(kind)
+
+
+def _make_op(pkg, S, kbloch=(0.0, 0.0, 0.0)):
+    g = S.grid
+    ph = tuple(np.exp(-1j * kbloch[w] * g.L[w]) for w in range(3))
+    A = pkg.FDFDOperator(g.N, S.omega, S.sdl_e, S.sdl_m, g.isbloch, ph)
+    A.set_eps(S.eps_diag, S.eps_off)
+    return A
+
+
+CASES = ["vacuum8", "spheres_odd", "ragged", "chunks", "bloch0", "blochk"]
+
+
+@pytest.mark.parametrize("kind", CASES)
+def test_matvec_parity(pkg, oracle, kind):
+    S, kw = _case(oracle, kind)
+    A = _make_op(pkg, S, **kw)
+    x = _rand(A.n, 11)
+    y_ref = S.A @ x
+    y = A @ x
+    err = np.linalg.norm(y - y_ref) / np.linalg.norm(y_ref)
+    assert err < TOL64, err
+    y32 = A.matvec(x, precision="c64")
+    err32 = np.linalg.norm(y32 - y_ref) / np.linalg.norm(y_ref)
+    assert err32 < TOL32, err32
+    A.close()
+
+
+@pytest.mark.parametrize("kind", ["vacuum8", "spheres_odd", "ragged", "bloch0"])
+def test_transpose_parity(pkg, oracle, kind):
+    S, kw = _case(oracle, kind)
+    A = _make_op(pkg, S, **kw)
+    x = _rand(A.n, 5)
+    y_ref = S.A.T @ x
+    y = A.T @ x
+    err = np.linalg.norm(y - y_ref) / np.linalg.norm(y_ref)
+    assert err < TOL64, err
+    A.close()
+
+
+def test_random_tensor_everywhere(pkg, oracle):
+    """Arbitrary ε diagonal and off-diagonal on every cell (walls included)."""
+    O = oracle
+    g = O.uniform_grid((11, 9, 12))
+    sdl_e, sdl_m = O.stretched_dl(g, 2 * np.pi / 6, ((2, 3, 1), (2, 1, 3)))
+    rng = np.random.default_rng(3)
+    ed = rng.uniform(1.0, 12.0, (11, 9, 12, 3))
+    eo = rng.uniform(-2.0, 2.0, (11, 9, 12, 3))
+    Ce, Cm = O.create_curls(g, sdl_e, sdl_m)
+    P = O.create_paramop(g, ed, eo, sdl_e, sdl_m)
+    om = 2 * np.pi / 6
+    Aref = O.create_A(om, P, Ce, Cm)
+    A = pkg.FDFDOperator(g.N, om, sdl_e, sdl_m)
+    A.set_eps(ed, eo)
+    x = _rand(A.n, 9)
+    y = A @ x
+    err = np.linalg.norm(y - Aref @ x) / np.linalg.norm(Aref @ x)
+    assert err < TOL64, err
+    A.close()
+
+
+def test_unit_vectors_index_map(pkg, oracle):
+    """Bit-exact DOF index map: A e_q has non-zeros exactly where column q of
+    the oracle's A does."""
+    S, _ = _case(oracle, "spheres_odd")
+    A = _make_op(pkg, S)
+    rng = np.random.default_rng(0)
+    Acsc = S.A.tocsc()
+    for q in rng.choice(A.n, 12, replace=False):
+        e = np.zeros(A.n, complex)
+        e[q] = 1.0
+        y = A @ e
+        col = Acsc[:, q].toarray().ravel()
+        assert np.array_equal(np.flatnonzero(np.abs(y) > 0), np.flatnonzero(np.abs(col) > 0)), q
+        assert np.allclose(y, col, rtol=1e-13, atol=1e-14)
+    A.close()
+
+
+def test_eps_tensor_layout(pkg, oracle):
+    """fdfd_set_eps_tensor reads the reference's (Nx,Ny,Nz,3,3) εarr."""
+    S, _ = _case(oracle, "spheres_odd")
+    g = S.grid
+    epsarr = np.zeros(g.N + (3, 3), complex)
+    for c in range(3):
+        epsarr[..., c, c] = S.eps_diag[..., c]
+    for p, (r, c) in enumerate(((0, 1), (1, 2), (2, 0))):
+        epsarr[..., r, c] = S.eps_off[..., p]
+        epsarr[..., c, r] = S.eps_off[..., p]
+    A = pkg.FDFDOperator(g.N, S.omega, S.sdl_e, S.sdl_m)
+    A.set_eps_tensor(epsarr)
+    ed, eo, _ = A.get_eps()
+    assert np.array_equal(ed, S.eps_diag) and np.array_equal(eo, S.eps_off)
+    x = _rand(A.n, 2)
+    assert np.linalg.norm(A @ x - S.A @ x) / np.linalg.norm(S.A @ x) < TOL64
+    bad = epsarr.copy()
+    bad[1, 1, 1, 0, 1] += 0.5
+    with pytest.raises(pkg.FDFDError):
+        A.set_eps_tensor(bad)
+    A.close()
