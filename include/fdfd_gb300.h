@@ -109,6 +109,7 @@ typedef struct {
   int32_t status;           /* FDFD_* status of the solve                              */
   double relres;            /* final true FP64 relative residual                        */
   double time_ms;           /* device time of the solve (CUDA events on the stream)    */
+  int64_t launches;         /* kernels launched for this solve (graph replays counted) */
 } fdfd_stats;
 
 /* ---- lifetime ------------------------------------------------------------

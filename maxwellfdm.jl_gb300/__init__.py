@@ -13,6 +13,7 @@ from .model import (EE, HH, Box, DesignRegion, ModelFull, Sphere, add_obj, add_s
                     create_A, create_b, create_linsys, create_stretched_dls, field_arr2vec, set_boundft, set_design,
                     set_kbloch, set_Npml, set_ωpml, vec2field_arr)
 from .operator import FDFDOperator
+from . import workloads
 from .sources import PlaneSrc, PointSrc, distweights
 
 __all__ = [

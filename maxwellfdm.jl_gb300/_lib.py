@@ -53,7 +53,8 @@ class fdfd_solve_opts(C.Structure):
 
 class fdfd_stats(C.Structure):
     _fields_ = [("iterations", C.c_int64), ("matvecs", C.c_int64), ("refinements", C.c_int32),
-                ("status", C.c_int32), ("relres", C.c_double), ("time_ms", C.c_double)]
+                ("status", C.c_int32), ("relres", C.c_double), ("time_ms", C.c_double),
+                ("launches", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

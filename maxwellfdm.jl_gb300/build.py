@@ -18,6 +18,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-Xptxas", "-O3"]
 SOURCES = ["stencil.cu", "blas1.cu", "solver.cu", "capi.cu", "setup.cu"]
+# setup.cu must round exactly like the CPU oracle (bit-identical object
+# indices and smoothing masks): no fused multiply-add contraction there.
+PER_SOURCE = {"setup.cu": ["--fmad=false"]}
 
 
 def _nvcc():
@@ -44,7 +47,7 @@ def build(verbose=False, force=False, extra_flags=()):
         src = os.path.join(CSRC, s)
         obj = os.path.join(BUILD, s.replace(".cu", ".o"))
         if force or _stale(obj, [src, __file__] + headers):
-            cmd = [nvcc, *ARCH, *NVCC_FLAGS, *extra_flags, "-c", src, "-o", obj]
+            cmd = [nvcc, *ARCH, *NVCC_FLAGS, *PER_SOURCE.get(s, []), *extra_flags, "-c", src, "-o", obj]
             jobs.append((s, cmd))
     def run(job):
         name, cmd = job

@@ -216,12 +216,14 @@ template <typename R>
 int bicg_p(fdfd_handle *h, const typename CT<R>::C *r, typename CT<R>::C *p, const typename CT<R>::C *v, long long n,
            const KScalars *sc) {
   k_bicg_p<R><<<vgrid(n), VB, 0, h->stream>>>(r, p, v, n, sc);
+  h->launches++;
   return cuda_check(h, cudaGetLastError(), "k_bicg_p");
 }
 template <typename R>
 int bicg_s(fdfd_handle *h, const typename CT<R>::C *r, const typename CT<R>::C *v, typename CT<R>::C *s, long long n,
            const KScalars *sc) {
   k_bicg_s<R><<<vgrid(n), VB, 0, h->stream>>>(r, v, s, n, sc);
+  h->launches++;
   return cuda_check(h, cudaGetLastError(), "k_bicg_s");
 }
 template <typename R>
@@ -230,6 +232,7 @@ int bicg_xr(fdfd_handle *h, typename CT<R>::C *x, const typename CT<R>::C *p, co
   int rc = ensure_red(h, RED_BLOCKS);
   if (rc) return rc;
   k_bicg_xr<R><<<vgrid(n), VB, 0, h->stream>>>(x, p, s, t, r, rh, n, h->red, sc);
+  h->launches++;
   return cuda_check(h, cudaGetLastError(), "k_bicg_xr");
 }
 template <typename R>
@@ -238,11 +241,13 @@ int cocg_xr(fdfd_handle *h, typename CT<R>::C *x, const typename CT<R>::C *p, co
   int rc = ensure_red(h, RED_BLOCKS);
   if (rc) return rc;
   k_cocg_xr<R><<<vgrid(n), VB, 0, h->stream>>>(x, p, q, r, w, n, h->red, sc);
+  h->launches++;
   return cuda_check(h, cudaGetLastError(), "k_cocg_xr");
 }
 template <typename R>
 int cocg_p(fdfd_handle *h, const typename CT<R>::C *r, typename CT<R>::C *p, long long n, const KScalars *sc) {
   k_cocg_p<R><<<vgrid(n), VB, 0, h->stream>>>(r, p, n, sc);
+  h->launches++;
   return cuda_check(h, cudaGetLastError(), "k_cocg_p");
 }
 template <typename R>
@@ -250,6 +255,7 @@ int dot(fdfd_handle *h, const typename CT<R>::C *a, const typename CT<R>::C *b, 
   int rc = ensure_red(h, RED_BLOCKS);
   if (rc) return rc;
   k_dot<R><<<vgrid(n), VB, 0, h->stream>>>(a, b, n, h->red, sc);
+  h->launches++;
   return cuda_check(h, cudaGetLastError(), "k_dot");
 }
 template <typename R>
@@ -258,27 +264,33 @@ int dot_u(fdfd_handle *h, const typename CT<R>::C *a, const typename CT<R>::C *b
   int rc = ensure_red(h, RED_BLOCKS);
   if (rc) return rc;
   k_dot_u<R><<<vgrid(n), VB, 0, h->stream>>>(a, b, w, n, h->red, fin, sc);
+  h->launches++;
   return cuda_check(h, cudaGetLastError(), "k_dot_u");
 }
 int accum(fdfd_handle *h, double2 *x64, float2 *x32, long long n) {
   k_accum<<<vgrid(n), VB, 0, h->stream>>>(x64, x32, n);
+  h->launches++;
   return cuda_check(h, cudaGetLastError(), "k_accum");
 }
 int accum64(fdfd_handle *h, double2 *x64, double2 *x, long long n) {
   k_accum64<<<vgrid(n), VB, 0, h->stream>>>(x64, x, n);
+  h->launches++;
   return cuda_check(h, cudaGetLastError(), "k_accum64");
 }
 int demote(fdfd_handle *h, float2 *y, const double2 *x, long long n) {
   k_demote<<<vgrid(n), VB, 0, h->stream>>>(y, x, n);
+  h->launches++;
   return cuda_check(h, cudaGetLastError(), "k_demote");
 }
 int promote(fdfd_handle *h, double2 *y, const float2 *x, long long n) {
   k_promote<<<vgrid(n), VB, 0, h->stream>>>(y, x, n);
+  h->launches++;
   return cuda_check(h, cudaGetLastError(), "k_promote");
 }
 template <typename R>
 int copy(fdfd_handle *h, typename CT<R>::C *y, const typename CT<R>::C *x, long long n) {
   k_copy<R><<<vgrid(n), VB, 0, h->stream>>>(y, x, n);
+  h->launches++;
   return cuda_check(h, cudaGetLastError(), "k_copy");
 }
 

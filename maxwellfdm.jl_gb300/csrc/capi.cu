@@ -468,6 +468,8 @@ static int check_opts(fdfd_handle *h, const fdfd_solve_opts *o) {
   if (o->precision == FDFD_PREC_MIXED && !(o->delta > 0.0 && o->delta < 1.0))
     return set_error(h, FDFD_ERR_ARG, "delta must be in (0, 1)");
   if (o->transpose && !transpose_ok(h)) return set_error(h, FDFD_ERR_UNSUPPORTED, "transpose with a Bloch phase");
+  if (o->method == FDFD_COCG && o->precision == FDFD_PREC_MIXED)
+    return set_error(h, FDFD_ERR_UNSUPPORTED, "COCG runs in FP64 only (its complex64 recurrence diverges)");
   if (o->method == FDFD_COCG && !transpose_ok(h))
     return set_error(h, FDFD_ERR_UNSUPPORTED, "COCG needs a complex-symmetric operator (no Bloch phase)");
   return FDFD_OK;

@@ -121,6 +121,7 @@ struct fdfd_handle {
   int red_blocks = 0;
   fdfd::Workspace *ws = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  long long launches = 0;  // kernels launched by this handle (graph replays included)
   std::string err;
 };
 

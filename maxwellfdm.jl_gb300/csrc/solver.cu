@@ -65,6 +65,7 @@ struct Workspace {
   KScalars *host = nullptr;  // pinned mirror
   cudaGraphExec_t gexec[2][2][2] = {};  // [precision][method][transpose]
   int gbatch[2][2][2] = {};
+  long long gkern[2][2][2] = {};        // kernels per graph replay
 };
 
 void free_workspace(fdfd_handle *h) {
@@ -211,7 +212,10 @@ static int run_batch(fdfd_handle *h, Workspace *ws, int method, bool tr, int bat
     TRY(ensure_red(h, apply_blocks(h)));
     cudaGraph_t g;
     TRY(cuda_check(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture"));
+    const long long l0 = h->launches;
     int rc = body();
+    ws->gkern[pi][mi][ti] = h->launches - l0;
+    h->launches = l0;
     cudaError_t e = cudaStreamEndCapture(h->stream, &g);
     if (rc) return rc;
     TRY(cuda_check(h, e, "end capture"));
@@ -220,6 +224,7 @@ static int run_batch(fdfd_handle *h, Workspace *ws, int method, bool tr, int bat
     TRY(cuda_check(h, e, "graph instantiate"));
     ws->gbatch[pi][mi][ti] = batch;
   }
+  h->launches += ws->gkern[pi][mi][ti];
   return cuda_check(h, cudaGraphLaunch(ge, h->stream), "graph launch");
 }
 
@@ -264,6 +269,7 @@ static int solve_impl(fdfd_handle *h, const double2 *b, double2 *x, const fdfd_s
   Workspace *ws = h->ws;
   const long long n = ws->n;
   TRY(cuda_check(h, cudaEventRecord(h->ev0, h->stream), "event"));
+  const long long launches0 = h->launches;
   if (o.x0_given) TRY(cuda_check(h, cudaMemcpyAsync(ws->x64, x, n * sizeof(double2), cudaMemcpyDeviceToDevice,
                                                     h->stream), "copy x0"));
   else TRY(cuda_check(h, cudaMemsetAsync(ws->x64, 0, n * sizeof(double2), h->stream), "memset x64"));
@@ -327,6 +333,13 @@ static int solve_impl(fdfd_handle *h, const double2 *b, double2 *x, const fdfd_s
           hs.rr_max = rr;
           hs.done = 0;
           hs.reason = 0;
+          if (o.method == FDFD_COCG) {
+            // COCG's ρ = rᵀ S r must describe the replaced residual
+            TRY(dot_u<R>(h, r, r, wvec<R>(ws), n, FIN_NONE, ws->scu));
+            KScalars t2;
+            TRY(read_scalars(h, ws->scu, &t2));
+            hs.rho = t2.dot0;
+          }
         }
         TRY(write_scalars(h, ws->sc, &hs));
       }
@@ -352,6 +365,7 @@ static int solve_impl(fdfd_handle *h, const double2 *b, double2 *x, const fdfd_s
   st.relres = std::sqrt(rr / bb);
   st.time_ms = ms;
   st.status = status;
+  st.launches = h->launches - launches0;
   if (status == FDFD_ERR_NOT_CONVERGED)
     return set_error(h, status, "solver reached maxit before the tolerance");
   if (status == FDFD_ERR_BREAKDOWN) return set_error(h, status, "Krylov breakdown persisted after restarts");

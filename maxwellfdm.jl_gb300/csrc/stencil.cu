@@ -89,6 +89,14 @@ __device__ __forceinline__ typename CT<R>::C load_e(const typename CT<R>::C *__r
   return val;
 }
 
+template <typename R, bool TRANSPOSE>
+__device__ __forceinline__ typename CT<R>::C own_e(const typename CT<R>::C *__restrict__ x, const Extra<R> &ex,
+                                                   long long cell, int c, int gi, int gj, int gk) {
+  typename CT<R>::C v = x[3 * cell + c];
+  if (TRANSPOSE) v = cmul(v, cinv(vol_e<R>(ex, c, gi, gj, gk)));
+  return v;
+}
+
 template <typename R>
 __device__ __forceinline__ int cidx(const OpArgs<R> &a, int v, int g) {
   // coefficient index for a (possibly ghost) H/E position along axis v
@@ -188,14 +196,19 @@ __global__ void __launch_bounds__(NTHR) k_apply(OpArgs<R> a, Extra<R> ex, const 
       C yx = csub(cmul(cey, csub(hz00, hzjm)), cmul(cez, csub(hyk, hykm)));
       C yy = csub(cmul(cez, csub(hxk, hxkm)), cmul(cex, csub(hz00, hzim)));
       C yz = csub(cmul(cex, csub(hyk, hyim)), cmul(cey, csub(hxk, hxjm)));
-      const C e_x = S.e[s0][0][ty + 1][tx + 1], e_y = S.e[s0][1][ty + 1][tx + 1], e_z = S.e[s0][2][ty + 1][tx + 1];
       const long long cell = gi + (long long)a.N[0] * gj + plane * k;
-      C dx = cscale(e_x, a.eps[cell]);
-      C dy = cscale(e_y, a.eps[a.ncell + cell]);
-      C dz = cscale(e_z, a.eps[2 * a.ncell + cell]);
       const bool pkz = !a.bloch[2] && k == 0;
       const bool pinx = pin_xy || pkz;
       const bool piny = pin_yx || pkz;
+      // the cell's own values: shared memory holds 0 for pinned DOFs (they
+      // do not enter the curl), but the ε term uses the true value
+      C e_x = S.e[s0][0][ty + 1][tx + 1], e_y = S.e[s0][1][ty + 1][tx + 1], e_z = S.e[s0][2][ty + 1][tx + 1];
+      if (pinx) e_x = own_e<R, TRANSPOSE>(x, ex, cell, 0, gi, gj, k);
+      if (piny) e_y = own_e<R, TRANSPOSE>(x, ex, cell, 1, gi, gj, k);
+      if (pinz) e_z = own_e<R, TRANSPOSE>(x, ex, cell, 2, gi, gj, k);
+      C dx = cscale(e_x, a.eps[cell]);
+      C dy = cscale(e_y, a.eps[a.ncell + cell]);
+      C dz = cscale(e_z, a.eps[2 * a.ncell + cell]);
       if (a.eoff != nullptr && (a.oflag == nullptr || a.oflag[tilecol * a.N[2] + k])) {
         const C wmz = a.wm[2][k], wpz = a.wp[2][k];
         // x output: corners (i', j, k), i' ∈ {i, i+1}
@@ -255,7 +268,10 @@ __global__ void __launch_bounds__(NTHR) k_apply(OpArgs<R> a, Extra<R> ex, const 
         acc0r.add(d0.x + d1.x + d2.x);
         acc0i.add(d0.y + d1.y + d2.y);
       } else if (EPI == EPI_DOT_TS) {
-        const C d0 = cdotc(yx, e_x), d1 = cdotc(yy, e_y), d2 = cdotc(yz, e_z);
+        // (t, s) with the unscaled input s (shared memory holds S⁻¹ s for Aᵀ)
+        const C sx = TRANSPOSE ? x[3 * cell] : e_x, sy = TRANSPOSE ? x[3 * cell + 1] : e_y,
+                sz = TRANSPOSE ? x[3 * cell + 2] : e_z;
+        const C d0 = cdotc(yx, sx), d1 = cdotc(yy, sy), d2 = cdotc(yz, sz);
         acc0r.add(d0.x + d1.x + d2.x);
         acc0i.add(d0.y + d1.y + d2.y);
         acc1r.add(yx.x * yx.x + yx.y * yx.y + yy.x * yy.x + yy.y * yy.y + yz.x * yz.x + yz.y * yz.y);
@@ -355,6 +371,7 @@ static int launch_t(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R>::
     if (rc) return rc;
   }
   k_apply<R, EPI, TR><<<grid, block, smem, h->stream>>>(a, ex, x, y, aux0, h->red, fin, sc);
+  h->launches++;
   return cuda_check(h, cudaGetLastError(), "k_apply launch");
 }
 

@@ -34,8 +34,7 @@ def sysx(oracle):
     return S, b, xd
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-@pytest.mark.parametrize("method", ["bicgstab", "cocg"])
+@pytest.mark.parametrize("precision,method", [("fp64", "bicgstab"), ("mixed", "bicgstab"), ("fp64", "cocg")])
 def test_solve_matches_direct(pkg, sysx, precision, method):
     S, b, xd = sysx
     A = _op(pkg, S)
@@ -95,4 +94,13 @@ def test_graph_and_plain_agree(pkg, sysx):
     x2, s2 = A.solve(b, tol=1e-6, precision="fp64", use_graph=False, check_every=10)
     assert s1[0]["iterations"] == s2[0]["iterations"]
     assert np.array_equal(x1, x2)
+    A.close()
+
+
+def test_mixed_cocg_rejected(pkg, sysx):
+    S, b, _ = sysx
+    A = _op(pkg, S)
+    with pytest.raises(pkg.FDFDError) as ei:
+        A.solve(b, precision="mixed", method="cocg")
+    assert ei.value.code == 2
     A.close()
