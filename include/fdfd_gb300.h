@@ -153,6 +153,12 @@ int fdfd_matvec(fdfd_handle *h, const double *x, double *y, int32_t precision);
 int fdfd_matvec_dev(fdfd_handle *h, const void *x, void *y, int32_t precision);
 /* y = Aᵀ x (transpose(A)*x; used by the adjoint). */
 int fdfd_matvec_transpose(fdfd_handle *h, const double *x, double *y, int32_t precision);
+/* r = b − A x and rnorm2 = ‖r‖₂², all complex128 device buffers (double2,
+ * 3·Ncell each), computed in FP64 by the operator kernel with a fused
+ * reduction (the true residual of create_linsys's system, model.jl:222-233,
+ * that a caller checks a solution against).  Returns once rnorm2 is on the
+ * host.  Uses the handle's reduction buffer. */
+int fdfd_residual_dev(fdfd_handle *h, const void *x, const void *b, void *r, double *rnorm2);
 
 /* ---- solve -----------------------------------------------------------------
  * x = A \ b to a true relative residual opts->tol (the reference leaves this

@@ -325,6 +325,12 @@ int fdfd_create(const fdfd_desc *d, fdfd_handle **out) {
   }
   if ((rc = finish_eps(h))) { fdfd_destroy(h); return rc; }
   if ((rc = ensure_red(h, apply_blocks(h)))) { fdfd_destroy(h); return rc; }
+  if (cudaMalloc(&h->util_sc, sizeof(KScalars)) != cudaSuccess) {
+    cudaGetLastError();
+    fdfd_destroy(h);
+    return set_error(nullptr, FDFD_ERR_NOMEM, "cudaMalloc(scalars) failed");
+  }
+  cudaMemsetAsync(h->util_sc, 0, sizeof(KScalars), h->stream);
   if ((rc = cuda_check(h, cudaStreamSynchronize(h->stream), "create sync"))) { fdfd_destroy(h); return rc; }
   *out = h;
   return FDFD_OK;
@@ -349,6 +355,7 @@ void fdfd_destroy(fdfd_handle *h) {
   cudaFree(h->vy32);
   cudaFree(h->red.part);
   cudaFree(h->red.count);
+  cudaFree(h->util_sc);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -457,6 +464,24 @@ int fdfd_matvec_dev(fdfd_handle *h, const void *x, void *y, int32_t precision) {
     return launch_apply_fin<double>(h, (const double2 *)x, (double2 *)y, EPI_STORE, nullptr, FIN_NONE, nullptr,
                                     false);
   return set_error(h, FDFD_ERR_ARG, "bad precision");
+}
+
+int fdfd_residual_dev(fdfd_handle *h, const void *x, const void *b, void *r, double *rnorm2) {
+  if (!h || !x || !b || !r || !rnorm2) return set_error(h, FDFD_ERR_ARG, "null argument");
+  cudaSetDevice(h->dev);
+  int rc = ensure_red(h, apply_blocks(h));
+  if (rc) return rc;
+  rc = launch_apply_fin<double>(h, (const double2 *)x, (double2 *)r, EPI_RESID, (const double2 *)b, FIN_NONE,
+                                h->util_sc, false);
+  if (rc) return rc;
+  KScalars hs;
+  rc = cuda_check(h, cudaMemcpyAsync(&hs, h->util_sc, sizeof(KScalars), cudaMemcpyDeviceToHost, h->stream),
+                  "D2H residual");
+  if (rc) return rc;
+  rc = cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
+  if (rc) return rc;
+  *rnorm2 = hs.dot0.x;
+  return FDFD_OK;
 }
 
 static int check_opts(fdfd_handle *h, const fdfd_solve_opts *o) {

@@ -122,6 +122,7 @@ struct fdfd_handle {
   fdfd::Workspace *ws = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   long long launches = 0;  // kernels launched by this handle (graph replays included)
+  fdfd::KScalars *util_sc = nullptr;  // finalisation target of one-off reductions
   std::string err;
 };
 

@@ -144,6 +144,13 @@ class FDFDOperator:
         """y = A x on device pointers (float2 for c64, double2 for c128), asynchronous on the handle's stream."""
         self._check(self._lib.fdfd_matvec_dev(self._h, C.c_void_p(x_ptr), C.c_void_p(y_ptr), _prec(precision)))
 
+    def residual_dev(self, x_ptr, b_ptr, r_ptr):
+        """r = b − A x on complex128 device buffers; returns ‖r‖₂² (FP64)."""
+        out = C.c_double()
+        self._check(self._lib.fdfd_residual_dev(self._h, C.c_void_p(x_ptr), C.c_void_p(b_ptr), C.c_void_p(r_ptr),
+                                                C.byref(out)))
+        return out.value
+
     # ---------------------------------------------------------------- solve
     def solve(self, b, tol=1e-6, precision="mixed", method="bicgstab", maxit=200000, x0=None, delta=0.1,
               check_every=50, transpose=False, use_graph=True):

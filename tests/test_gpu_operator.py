@@ -149,3 +149,22 @@ def test_eps_tensor_layout(pkg, oracle):
     with pytest.raises(pkg.FDFDError):
         A.set_eps_tensor(bad)
     A.close()
+
+
+def test_residual_dev(pkg, oracle):
+    """fdfd_residual_dev: r = b − A x and ‖r‖² in FP64 on device buffers."""
+    torch = pytest.importorskip("torch")
+    S, _ = _case(oracle, "spheres_odd")
+    A = _make_op(pkg, S)
+    x = _rand(A.n, 21)
+    b = _rand(A.n, 22)
+    dev = torch.device("cuda", 0)
+    xd = torch.from_numpy(x.view(np.float64).reshape(-1, 2)).to(dev)
+    bd = torch.from_numpy(b.view(np.float64).reshape(-1, 2)).to(dev)
+    rd = torch.empty_like(xd)
+    rr = A.residual_dev(xd.data_ptr(), bd.data_ptr(), rd.data_ptr())
+    r_ref = b - S.A @ x
+    r = rd.cpu().numpy().view(np.complex128).reshape(-1)
+    assert np.linalg.norm(r - r_ref) / np.linalg.norm(r_ref) < TOL64
+    assert abs(rr - np.vdot(r_ref, r_ref).real) / np.vdot(r_ref, r_ref).real < 1e-12
+    A.close()
