@@ -82,6 +82,8 @@ SIGNATURES = {
                                  C.POINTER(fdfd_stats)]),
     "fdfd_default_opts": (None, [C.POINTER(fdfd_solve_opts)]),
     "fdfd_residual_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
+    "fdfd_residual_dev_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.POINTER(C.c_double)]),
     "fdfd_eps_grad": (C.c_int, [C.c_void_p, _dp, _dp, _dp, C.POINTER(fdfd_solve_opts), C.POINTER(fdfd_stats)]),
 }
 

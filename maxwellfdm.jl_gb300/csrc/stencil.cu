@@ -375,6 +375,37 @@ static int launch_t(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R>::
   return cuda_check(h, cudaGetLastError(), "k_apply launch");
 }
 
+// FP64 residual launcher whose block partials, arrival counter and
+// finalisation scalars live in caller-provided device memory (used by the
+// allocation-free entry point).  Fails if the grid needs more than
+// `max_blocks` partial slots.
+int launch_residual_ext(fdfd_handle *h, const double2 *x, double2 *r, const double2 *b, RedBuf red, int max_blocks,
+                        KScalars *sc) {
+  const size_t smem = sizeof(StencilSmem<double>);
+  cudaError_t e =
+      cudaFuncSetAttribute(k_apply<double, EPI_RESID, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return cuda_check(h, e, "cudaFuncSetAttribute(k_apply)");
+  const int kc = kchunk_for(h);
+  dim3 grid((h->N[0] + TX - 1) / TX, (h->N[1] + TY - 1) / TY, (h->N[2] + kc - 1) / kc);
+  if ((long long)grid.x * grid.y * grid.z > max_blocks)
+    return set_error(h, FDFD_ERR_ARG, "grid needs more thread blocks than the fixed reduction scratch holds");
+  OpArgs<double> a = op_args<double>(h);
+  Extra<double> ex;
+  ex.kchunk = kc;
+  const double2 *coef = h->coef64;
+  const int st = h->coef_stride;
+  for (int w = 0; w < 3; ++w) {
+    ex.sdle[w] = coef + 4 * st + h->coef_off[w];
+    ex.sdlm[w] = coef + 5 * st + h->coef_off[w];
+    ex.ph[w] = make_double2(h->e_ikl[w][0], h->e_ikl[w][1]);
+    const double d2 = h->e_ikl[w][0] * h->e_ikl[w][0] + h->e_ikl[w][1] * h->e_ikl[w][1];
+    ex.phinv[w] = make_double2(h->e_ikl[w][0] / d2, -h->e_ikl[w][1] / d2);
+  }
+  k_apply<double, EPI_RESID, false><<<grid, dim3(TX, TY, 1), smem, h->stream>>>(a, ex, x, r, b, red, FIN_NONE, sc);
+  h->launches++;
+  return cuda_check(h, cudaGetLastError(), "k_apply launch");
+}
+
 // Full-control launcher (epilogue + finalisation mode).
 template <typename R>
 int launch_apply_fin(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R>::C *y, int epi,
