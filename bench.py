@@ -251,12 +251,15 @@ def run_ours(args):
     yout = torch.empty_like(xin)
     xin64 = torch.randn(n, 2, device=dev, dtype=torch.float64)
     yout64 = torch.empty_like(xin64)
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    # L2 flush by READING 256 MiB (> 129 MB L2): evicts the operands and
+    # leaves only clean lines, so the timed launch is not charged for the
+    # write-back of a flush buffer
+    flush = torch.ones(64 << 20, dtype=torch.float32, device=dev)
     def timed(prec, xx, yy, reps):
         ts = []
         with torch.cuda.stream(stream):
             for r in range(reps + 2):
-                flush.zero_()
+                flush.sum()
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
@@ -303,8 +306,9 @@ def run_ours(args):
             "vs_baseline": None, "dtype": "c64 (FP64 reductions and residual replacement)",
             "data": "synthetic (seeded spheres, seed 1000+rank)",
             "config": {"workload": WORKLOAD, "cells": A.ncell, "unknowns": n, "solver": "BiCGSTAB",
-                       "tol": tol, "l2": "working set > L2 (8 c64 + 3 c128 vectors = 0.5 GB); L2 flushed "
-                                         "before each roofline launch", "parallelism": "replicas" if ws > 1 else "1 GPU"},
+                       "tol": tol, "l2": "solve working set > L2 (8 c64 + 3 c128 vectors = 0.5 GB); L2 flushed "
+                                         "by a 256 MiB read before each roofline launch",
+                       "parallelism": "replicas" if ws > 1 else "1 GPU"},
             "fp64_time_s": t_fp64, "mixed_speedup_vs_fp64": t_fp64 / t_mixed,
             "iterations": stats[-1]["iterations"], "fp64_iterations": st64["iterations"],
             "refinements": stats[-1]["refinements"], "relres": stats[-1]["relres"],
@@ -328,6 +332,49 @@ def run_ours(args):
     return 0
 
 
+def run_profile(args):
+    """Small, self-terminating runs for ncu: `matvec` applies the complex64
+    operator `--reps` times on a sphere model of size `--grid`; `solve` runs
+    the bench workload's mixed solve capped at `--maxit` iterations."""
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    dev = torch.device("cuda", 0)
+    if args.profile == "matvec":
+        N = tuple(int(v) for v in args.grid.split(","))
+        g = pkg.uniform_grid(N)
+        om = 2 * np.pi / 16
+        mdl = pkg.ModelFull(g)
+        pkg.set_ωpml(mdl, om)
+        pkg.set_Npml(mdl, ((10,) * 3, (10,) * 3))
+        rng = np.random.default_rng(7)
+        for c, r, e in pkg.workloads._spheres(rng, N, 10, 40, 3.0, 8.0, [12.25]):
+            pkg.add_obj(mdl, "dielectric", pkg.Sphere(c, r), ε=e)
+        A = pkg.create_A(mdl, om)
+        prec = args.precision
+        dt = torch.float32 if prec == "c64" else torch.float64
+        x = torch.randn(A.n, 2, device=dev, dtype=dt)
+        y = torch.empty_like(x)
+        for _ in range(args.reps):
+            A.matvec_dev(x.data_ptr(), y.data_ptr(), prec)
+        A.sync()
+        print(f"profile matvec {N} {prec} x{args.reps} done")
+    else:
+        mdl, om = pkg.workloads.config2()
+        A = pkg.create_A(mdl, om)
+        b = pkg.create_b(mdl, om)
+        bd = torch.from_numpy(b.view(np.float64).reshape(-1, 2)).to(dev)
+        xd = torch.zeros_like(bd)
+        try:
+            st = A.solve_dev(bd.data_ptr(), xd.data_ptr(), tol=1e-6, precision="mixed", maxit=args.maxit,
+                             check_every=10)
+        except pkg.FDFDError as e:
+            st = getattr(e, "stats", None) or str(e)
+        print(f"profile solve maxit={args.maxit}: {st}")
+    A.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -335,7 +382,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--profile", choices=["matvec", "solve"], help="short run for ncu (no bench line)")
+    ap.add_argument("--grid", default="256,256,128")
+    ap.add_argument("--precision", default="c64", choices=["c64", "c128"])
+    ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--maxit", type=int, default=100)
     args = ap.parse_args()
+    if args.profile:
+        return run_profile(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -86,12 +86,14 @@ __global__ void __launch_bounds__(VB) k_bicg_xr(typename CT<R>::C *x, const type
   block_reduce_finalise<VB>(make_double2(a0r.get(), a0i.get()), make_double2(a1.get(), 0.0), red, FIN_XR, sc);
 }
 
-// COCG (symmetric form, right-preconditioned by diagonal d):
-//   x += α p ; r −= α q ; rᵀ z and ‖r‖² with z = d∘r  → FIN_COCG_R
+// Jacobi-preconditioned COCG on the S-symmetric operator (S = V_E, so S·A
+// is complex symmetric; z = D⁻¹ r with D = diag(A)):
+//   x += α p ; r −= α q ; ρ' = rᵀ S z and ‖r‖²  → FIN_COCG_R
 template <typename R>
 __global__ void __launch_bounds__(VB) k_cocg_xr(typename CT<R>::C *x, const typename CT<R>::C *__restrict__ p,
                                                 const typename CT<R>::C *__restrict__ q, typename CT<R>::C *r,
-                                                const typename CT<R>::C *__restrict__ wgt, long long n, RedBuf red,
+                                                const typename CT<R>::C *__restrict__ wgt,
+                                                const typename CT<R>::C *__restrict__ dinv, long long n, RedBuf red,
                                                 KScalars *sc) {
   using C = typename CT<R>::C;
   if (sc->done) return;
@@ -101,8 +103,8 @@ __global__ void __launch_bounds__(VB) k_cocg_xr(typename CT<R>::C *x, const type
     x[i] = cadd(x[i], cmul(al, p[i]));
     const C ri = csub(r[i], cmul(al, q[i]));
     r[i] = ri;
-    const C wr = cmul(wgt[i], ri);  // S r
-    const C d = cmul(ri, wr);       // rᵀ S r (unconjugated)
+    const C zi = cmul(dinv[i], ri);
+    const C d = cmul(cmul(wgt[i], ri), zi);  // rᵀ S z (unconjugated)
     a0r.add(d.x);
     a0i.add(d.y);
     a1.add(ri.x * ri.x + ri.y * ri.y);
@@ -110,15 +112,24 @@ __global__ void __launch_bounds__(VB) k_cocg_xr(typename CT<R>::C *x, const type
   block_reduce_finalise<VB>(make_double2(a0r.get(), a0i.get()), make_double2(a1.get(), 0.0), red, FIN_COCG_R, sc);
 }
 
-// COCG direction: p = r + β p
+// COCG direction: p = D⁻¹ r + β p
 template <typename R>
-__global__ void __launch_bounds__(VB) k_cocg_p(const typename CT<R>::C *__restrict__ r, typename CT<R>::C *p,
+__global__ void __launch_bounds__(VB) k_cocg_p(const typename CT<R>::C *__restrict__ r,
+                                               const typename CT<R>::C *__restrict__ dinv, typename CT<R>::C *p,
                                                long long n, const KScalars *sc) {
   using C = typename CT<R>::C;
   if (sc->done) return;
   const C be = tocr<R>(sc->beta);
   for (long long i = blockIdx.x * (long long)VB + threadIdx.x; i < n; i += (long long)gridDim.x * VB)
-    p[i] = cadd(r[i], cmul(be, p[i]));
+    p[i] = cadd(cmul(dinv[i], r[i]), cmul(be, p[i]));
+}
+
+// y = a ∘ b (elementwise complex product)
+template <typename R>
+__global__ void __launch_bounds__(VB) k_vmul(typename CT<R>::C *y, const typename CT<R>::C *__restrict__ a,
+                                             const typename CT<R>::C *__restrict__ b, long long n) {
+  for (long long i = blockIdx.x * (long long)VB + threadIdx.x; i < n; i += (long long)gridDim.x * VB)
+    y[i] = cmul(a[i], b[i]);
 }
 
 // Generic reductions: mode 0: (a, b) Hermitian and ‖a‖²;  mode 1: aᵀ S a
@@ -237,18 +248,26 @@ int bicg_xr(fdfd_handle *h, typename CT<R>::C *x, const typename CT<R>::C *p, co
 }
 template <typename R>
 int cocg_xr(fdfd_handle *h, typename CT<R>::C *x, const typename CT<R>::C *p, const typename CT<R>::C *q,
-            typename CT<R>::C *r, const typename CT<R>::C *w, long long n, KScalars *sc) {
+            typename CT<R>::C *r, const typename CT<R>::C *w, const typename CT<R>::C *dinv, long long n,
+            KScalars *sc) {
   int rc = ensure_red(h, RED_BLOCKS);
   if (rc) return rc;
-  k_cocg_xr<R><<<vgrid(n), VB, 0, h->stream>>>(x, p, q, r, w, n, h->red, sc);
+  k_cocg_xr<R><<<vgrid(n), VB, 0, h->stream>>>(x, p, q, r, w, dinv, n, h->red, sc);
   h->launches++;
   return cuda_check(h, cudaGetLastError(), "k_cocg_xr");
 }
 template <typename R>
-int cocg_p(fdfd_handle *h, const typename CT<R>::C *r, typename CT<R>::C *p, long long n, const KScalars *sc) {
-  k_cocg_p<R><<<vgrid(n), VB, 0, h->stream>>>(r, p, n, sc);
+int cocg_p(fdfd_handle *h, const typename CT<R>::C *r, const typename CT<R>::C *dinv, typename CT<R>::C *p,
+           long long n, const KScalars *sc) {
+  k_cocg_p<R><<<vgrid(n), VB, 0, h->stream>>>(r, dinv, p, n, sc);
   h->launches++;
   return cuda_check(h, cudaGetLastError(), "k_cocg_p");
+}
+template <typename R>
+int vmul(fdfd_handle *h, typename CT<R>::C *y, const typename CT<R>::C *a, const typename CT<R>::C *b, long long n) {
+  k_vmul<R><<<vgrid(n), VB, 0, h->stream>>>(y, a, b, n);
+  h->launches++;
+  return cuda_check(h, cudaGetLastError(), "k_vmul");
 }
 template <typename R>
 int dot(fdfd_handle *h, const typename CT<R>::C *a, const typename CT<R>::C *b, long long n, KScalars *sc) {
@@ -300,8 +319,10 @@ int copy(fdfd_handle *h, typename CT<R>::C *y, const typename CT<R>::C *x, long 
   template int bicg_xr<R>(fdfd_handle *, CT<R>::C *, const CT<R>::C *, const CT<R>::C *, const CT<R>::C *,          \
                           CT<R>::C *, const CT<R>::C *, long long, KScalars *);                                       \
   template int cocg_xr<R>(fdfd_handle *, CT<R>::C *, const CT<R>::C *, const CT<R>::C *, CT<R>::C *,                 \
-                          const CT<R>::C *, long long, KScalars *);                                                   \
-  template int cocg_p<R>(fdfd_handle *, const CT<R>::C *, CT<R>::C *, long long, const KScalars *);                 \
+                          const CT<R>::C *, const CT<R>::C *, long long, KScalars *);                                 \
+  template int cocg_p<R>(fdfd_handle *, const CT<R>::C *, const CT<R>::C *, CT<R>::C *, long long,                  \
+                         const KScalars *);                                                                           \
+  template int vmul<R>(fdfd_handle *, CT<R>::C *, const CT<R>::C *, const CT<R>::C *, long long);                   \
   template int dot<R>(fdfd_handle *, const CT<R>::C *, const CT<R>::C *, long long, KScalars *);                     \
   template int dot_u<R>(fdfd_handle *, const CT<R>::C *, const CT<R>::C *, const CT<R>::C *, long long, int,        \
                         KScalars *);                                                                                  \

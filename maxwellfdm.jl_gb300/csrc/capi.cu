@@ -7,8 +7,10 @@
 // create_stretched_∆ls (:135-152) and the material tensor εarr
 // (:64, full.jl:16-70) — once, and every application or solve runs on the
 // GPU against device-resident data.
+#include <algorithm>
 #include <cmath>
 #include <complex>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -32,35 +34,82 @@ int cuda_check(fdfd_handle *h, cudaError_t e, const char *what) {
   return set_error(h, FDFD_ERR_CUDA, m);
 }
 
+int check_dev_err(fdfd_handle *h) {
+  if (!h->dev_err) return FDFD_OK;
+  int v = 0;
+  int rc = cuda_check(h, cudaMemcpy(&v, h->dev_err, sizeof(int), cudaMemcpyDeviceToHost), "read error flag");
+  if (rc) return rc;
+  if (v == 0) return FDFD_OK;
+  cudaMemset(h->dev_err, 0, sizeof(int));
+  return set_error(h, FDFD_ERR_TIMEOUT, "a bounded device-side wait gave up (a TMA copy did not complete)");
+}
+
 int solve_dev_impl(fdfd_handle *h, const double2 *b, double2 *x, const fdfd_solve_opts *o, fdfd_stats *st);
 int demote(fdfd_handle *, float2 *, const double2 *, long long);
 int promote(fdfd_handle *, double2 *, const float2 *, long long);
 
 using cd = std::complex<double>;
 
-// S = V_E per DOF (the symmetriser of A): V_E(c) = s∆lₘ[c][g_c] Π_{v≠c} s∆lₑ[v][g_v]
-__global__ void k_weights(const double2 *coef, int st, int o0, int o1, int o2, int N0, int N1, int N2, double2 *w64,
-                          float2 *w32) {
-  const long long ncell = (long long)N0 * N1 * N2;
+// Per-DOF factors of the COCG solver:
+//   S = V_E (the symmetriser of A): V_E(c) = s∆lₘ[c][g_c] Π_{v≠c} s∆lₑ[v][g_v];
+//   D⁻¹ = 1/diag(A), diag(A)_c = Σ_{v≠c} (1/s∆lₑ[v][g_v])·(1/s∆lₘ[v][g_v] +
+//   1/s∆lₘ[v][g_v−1]) − ω² ε_cc, and −ω² ε_cc alone on pinned DOFs.
+struct WeightArgs {
+  const double2 *coef;
+  const double *eps;
+  int st, off[3], N[3], bloch[3];
+  double2 w2;
+};
+
+__global__ void k_weights(WeightArgs a, double2 *w64, float2 *w32, double2 *d64, float2 *d32) {
+  const long long ncell = (long long)a.N[0] * a.N[1] * a.N[2];
   for (long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x; cell < ncell;
        cell += (long long)gridDim.x * blockDim.x) {
-    const int g[3] = {(int)(cell % N0), (int)((cell / N0) % N1), (int)(cell / ((long long)N0 * N1))};
-    const int off[3] = {o0, o1, o2};
+    const int g[3] = {(int)(cell % a.N[0]), (int)((cell / a.N[0]) % a.N[1]), (int)(cell / ((long long)a.N[0] * a.N[1]))};
     for (int c = 0; c < 3; ++c) {
       double2 v = make_double2(1.0, 0.0);
-      for (int a = 0; a < 3; ++a) {
-        const double2 f = coef[(a == c ? 5 : 4) * st + off[a] + g[a]];
+      for (int ax = 0; ax < 3; ++ax) {
+        const double2 f = a.coef[(ax == c ? 5 : 4) * a.st + a.off[ax] + g[ax]];
         v = make_double2(v.x * f.x - v.y * f.y, v.x * f.y + v.y * f.x);
       }
       if (w64) w64[3 * cell + c] = v;
       if (w32) w32[3 * cell + c] = make_float2((float)v.x, (float)v.y);
+      bool pinned = false;
+      double2 d = make_double2(0.0, 0.0);
+      for (int ax = 0; ax < 3; ++ax) {
+        if (ax == c) continue;
+        if (!a.bloch[ax] && g[ax] == 0) pinned = true;
+        const int gm = g[ax] > 0 ? g[ax] - 1 : a.N[ax] - 1;
+        const double2 ce = a.coef[1 * a.st + a.off[ax] + g[ax]];
+        const double2 c0 = a.coef[0 * a.st + a.off[ax] + g[ax]], c1 = a.coef[0 * a.st + a.off[ax] + gm];
+        const double2 s = make_double2(c0.x + c1.x, c0.y + c1.y);
+        d.x += ce.x * s.x - ce.y * s.y;
+        d.y += ce.x * s.y + ce.y * s.x;
+      }
+      if (pinned) d = make_double2(0.0, 0.0);
+      const double e = a.eps[c * ncell + cell];
+      d.x -= a.w2.x * e;
+      d.y -= a.w2.y * e;
+      const double dd = d.x * d.x + d.y * d.y;
+      const double2 inv = make_double2(d.x / dd, -d.y / dd);
+      if (d64) d64[3 * cell + c] = inv;
+      if (d32) d32[3 * cell + c] = make_float2((float)inv.x, (float)inv.y);
     }
   }
 }
 
-int build_weights(fdfd_handle *h, double2 *w64, float2 *w32) {
-  k_weights<<<152 * 4, 256, 0, h->stream>>>(h->coef64, h->coef_stride, (int)h->coef_off[0], (int)h->coef_off[1],
-                                            (int)h->coef_off[2], h->N[0], h->N[1], h->N[2], w64, w32);
+int build_weights(fdfd_handle *h, double2 *w64, float2 *w32, double2 *d64, float2 *d32) {
+  WeightArgs a;
+  a.coef = h->coef64;
+  a.eps = h->eps64;
+  a.st = h->coef_stride;
+  for (int w = 0; w < 3; ++w) {
+    a.off[w] = (int)h->coef_off[w];
+    a.N[w] = h->N[w];
+    a.bloch[w] = h->bloch[w];
+  }
+  a.w2 = make_double2(h->w2[0], h->w2[1]);
+  k_weights<<<152 * 4, 256, 0, h->stream>>>(a, w64, w32, d64, d32);
   return cuda_check(h, cudaGetLastError(), "k_weights");
 }
 
@@ -211,7 +260,9 @@ static int matvec_host(fdfd_handle *h, const double *x, double *y, int precision
   }
   rc = cuda_check(h, cudaMemcpyAsync(y, h->vy64, n * sizeof(double2), cudaMemcpyDeviceToHost, h->stream), "D2H y");
   if (rc) return rc;
-  return cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
+  rc = cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
+  if (rc) return rc;
+  return check_dev_err(h);
 }
 
 }  // namespace fdfd
@@ -324,13 +375,26 @@ int fdfd_create(const fdfd_desc *d, fdfd_handle **out) {
     cudaMemcpy(h->eps64, ones.data(), ones.size() * sizeof(double), cudaMemcpyHostToDevice);
   }
   if ((rc = finish_eps(h))) { fdfd_destroy(h); return rc; }
-  if ((rc = ensure_red(h, apply_blocks(h)))) { fdfd_destroy(h); return rc; }
   if (cudaMalloc(&h->util_sc, sizeof(KScalars)) != cudaSuccess) {
     cudaGetLastError();
     fdfd_destroy(h);
     return set_error(nullptr, FDFD_ERR_NOMEM, "cudaMalloc(scalars) failed");
   }
   cudaMemsetAsync(h->util_sc, 0, sizeof(KScalars), h->stream);
+  if (cudaMalloc(&h->dev_err, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    fdfd_destroy(h);
+    return set_error(nullptr, FDFD_ERR_NOMEM, "cudaMalloc(error flag) failed");
+  }
+  cudaMemsetAsync(h->dev_err, 0, sizeof(int), h->stream);
+  {
+    const char *ev = std::getenv("FDFD_DISABLE_TMA");
+    h->tma_disabled = ev != nullptr && ev[0] != '\0' && ev[0] != '0';
+    const char *kc = std::getenv("FDFD_KCHUNK");
+    if (kc != nullptr) h->kc_force = std::max(1, std::min(std::atoi(kc), h->N[2]));
+  }
+  if ((rc = autotune_kchunk(h))) { fdfd_destroy(h); return rc; }
+  if ((rc = ensure_red(h, apply_blocks(h)))) { fdfd_destroy(h); return rc; }
   if ((rc = cuda_check(h, cudaStreamSynchronize(h->stream), "create sync"))) { fdfd_destroy(h); return rc; }
   *out = h;
   return FDFD_OK;
@@ -356,6 +420,7 @@ void fdfd_destroy(fdfd_handle *h) {
   cudaFree(h->red.part);
   cudaFree(h->red.count);
   cudaFree(h->util_sc);
+  cudaFree(h->dev_err);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -366,7 +431,9 @@ void *fdfd_stream(fdfd_handle *h) { return h ? (void *)h->stream : nullptr; }
 
 int fdfd_sync(fdfd_handle *h) {
   if (!h) return set_error(nullptr, FDFD_ERR_ARG, "null handle");
-  return cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
+  int rc = cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
+  if (rc) return rc;
+  return check_dev_err(h);
 }
 
 int fdfd_set_eps(fdfd_handle *h, const double *eps_diag, const double *eps_off) {
@@ -494,7 +561,9 @@ static int check_opts(fdfd_handle *h, const fdfd_solve_opts *o) {
     return set_error(h, FDFD_ERR_ARG, "delta must be in (0, 1)");
   if (o->transpose && !transpose_ok(h)) return set_error(h, FDFD_ERR_UNSUPPORTED, "transpose with a Bloch phase");
   if (o->method == FDFD_COCG && o->precision == FDFD_PREC_MIXED)
-    return set_error(h, FDFD_ERR_UNSUPPORTED, "COCG runs in FP64 only (its complex64 recurrence diverges)");
+    return set_error(h, FDFD_ERR_UNSUPPORTED, "COCG runs in FP64 only (its complex64 recurrence does not converge)");
+  if (o->method == FDFD_COCG && o->transpose)
+    return set_error(h, FDFD_ERR_UNSUPPORTED, "COCG solves the forward system only (use BiCGSTAB for Aᵀ)");
   if (o->method == FDFD_COCG && !transpose_ok(h))
     return set_error(h, FDFD_ERR_UNSUPPORTED, "COCG needs a complex-symmetric operator (no Bloch phase)");
   return FDFD_OK;

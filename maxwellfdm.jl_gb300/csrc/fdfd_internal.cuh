@@ -65,6 +65,7 @@ enum EpiKind : int {
   EPI_RESID = 1,        // y = b - A x, accumulate ‖y‖²       (aux0 = b)
   EPI_DOT_AUX = 2,      // y = A x, accumulate conj(aux0)·y     (aux0 = r̂)
   EPI_DOT_TS = 3,       // y = A x, accumulate conj(y)·x, ‖y‖²  (t = A s)
+  EPI_DOT_SU = 4,       // y = A x, accumulate Σ V_E·x·y (unconjugated, COCG's pᵀ S q)
 };
 
 // Reduction slots used by the fused kernels: each kernel accumulates up to
@@ -123,6 +124,10 @@ struct fdfd_handle {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   long long launches = 0;  // kernels launched by this handle (graph replays included)
   fdfd::KScalars *util_sc = nullptr;  // finalisation target of one-off reductions
+  int *dev_err = nullptr;             // set by a kernel whose bounded wait gave up
+  bool tma_disabled = false;          // FDFD_DISABLE_TMA=1: plain-load operator kernel only
+  int kc[2] = {0, 0};                 // tuned z-chunk length: [complex128, complex64]
+  int kc_force = 0;                   // FDFD_KCHUNK: fixed z-chunk length (no tuning)
   std::string err;
 };
 
@@ -130,6 +135,9 @@ namespace fdfd {
 
 int set_error(fdfd_handle *h, int code, const std::string &msg);
 int cuda_check(fdfd_handle *h, cudaError_t e, const char *what);
+// FDFD_ERR_TIMEOUT (and clears the flag) if a kernel reported a bounded
+// wait that gave up; call after the stream has been synchronised.
+int check_dev_err(fdfd_handle *h);
 
 template <typename R> OpArgs<R> op_args(const fdfd_handle *h);
 
@@ -141,6 +149,8 @@ int launch_apply_fin(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R>:
                      const typename CT<R>::C *aux0, int fin, KScalars *sc, bool transpose);
 // number of blocks launch_apply uses (reduction buffer sizing)
 int apply_blocks(const fdfd_handle *h);
+// pick the z-chunk length per precision by timing (stencil.cu)
+int autotune_kchunk(fdfd_handle *h);
 
 // Finalise per-block partials; defined in blas1.cu
 int ensure_red(fdfd_handle *h, int blocks);

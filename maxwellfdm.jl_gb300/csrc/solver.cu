@@ -32,9 +32,12 @@ int bicg_xr(fdfd_handle *, typename CT<R>::C *, const typename CT<R>::C *, const
             const typename CT<R>::C *, typename CT<R>::C *, const typename CT<R>::C *, long long, KScalars *);
 template <typename R>
 int cocg_xr(fdfd_handle *, typename CT<R>::C *, const typename CT<R>::C *, const typename CT<R>::C *,
-            typename CT<R>::C *, const typename CT<R>::C *, long long, KScalars *);
+            typename CT<R>::C *, const typename CT<R>::C *, const typename CT<R>::C *, long long, KScalars *);
 template <typename R>
-int cocg_p(fdfd_handle *, const typename CT<R>::C *, typename CT<R>::C *, long long, const KScalars *);
+int cocg_p(fdfd_handle *, const typename CT<R>::C *, const typename CT<R>::C *, typename CT<R>::C *, long long,
+           const KScalars *);
+template <typename R>
+int vmul(fdfd_handle *, typename CT<R>::C *, const typename CT<R>::C *, const typename CT<R>::C *, long long);
 template <typename R>
 int dot(fdfd_handle *, const typename CT<R>::C *, const typename CT<R>::C *, long long, KScalars *);
 template <typename R>
@@ -46,7 +49,7 @@ int accum(fdfd_handle *, double2 *, float2 *, long long);
 int accum64(fdfd_handle *, double2 *, double2 *, long long);
 int demote(fdfd_handle *, float2 *, const double2 *, long long);
 int promote(fdfd_handle *, double2 *, const float2 *, long long);
-int build_weights(fdfd_handle *h, double2 *w64, float2 *w32);
+int build_weights(fdfd_handle *h, double2 *w64, float2 *w32, double2 *d64, float2 *d32);
 
 #define TRY(x)              \
   do {                      \
@@ -59,8 +62,8 @@ struct Workspace {
   double2 *x64 = nullptr, *r64 = nullptr;
   float2 *f[7] = {nullptr};
   double2 *d[7] = {nullptr};
-  double2 *w64 = nullptr;
-  float2 *w32 = nullptr;
+  double2 *w64 = nullptr, *dj64 = nullptr;  // COCG: S weights and Jacobi factors 1/diag(A)
+  float2 *w32 = nullptr, *dj32 = nullptr;
   KScalars *sc = nullptr, *scu = nullptr;
   KScalars *host = nullptr;  // pinned mirror
   cudaGraphExec_t gexec[2][2][2] = {};  // [precision][method][transpose]
@@ -79,6 +82,8 @@ void free_workspace(fdfd_handle *h) {
   }
   cudaFree(ws->w64);
   cudaFree(ws->w32);
+  cudaFree(ws->dj64);
+  cudaFree(ws->dj32);
   cudaFree(ws->sc);
   cudaFree(ws->scu);
   if (ws->host) cudaFreeHost(ws->host);
@@ -115,9 +120,16 @@ static int ensure_ws(fdfd_handle *h, bool mixed, int method) {
     else TRY(alloc(h, (void **)&ws->d[i], n * sizeof(double2), "inner vector (c128)"));
   }
   if (method == FDFD_COCG) {
-    if (mixed) TRY(alloc(h, (void **)&ws->w32, n * sizeof(float2), "weights"));
-    else TRY(alloc(h, (void **)&ws->w64, n * sizeof(double2), "weights"));
-    TRY(build_weights(h, mixed ? nullptr : ws->w64, mixed ? ws->w32 : nullptr));
+    // rebuilt on every solve: the Jacobi factors follow the current ε
+    if (mixed) {
+      TRY(alloc(h, (void **)&ws->w32, n * sizeof(float2), "weights"));
+      TRY(alloc(h, (void **)&ws->dj32, n * sizeof(float2), "Jacobi factors"));
+    } else {
+      TRY(alloc(h, (void **)&ws->w64, n * sizeof(double2), "weights"));
+      TRY(alloc(h, (void **)&ws->dj64, n * sizeof(double2), "Jacobi factors"));
+    }
+    TRY(build_weights(h, mixed ? nullptr : ws->w64, mixed ? ws->w32 : nullptr, mixed ? nullptr : ws->dj64,
+                      mixed ? ws->dj32 : nullptr));
   }
   TRY(alloc(h, (void **)&ws->sc, sizeof(KScalars), "scalars"));
   TRY(alloc(h, (void **)&ws->scu, sizeof(KScalars), "scalars"));
@@ -139,6 +151,9 @@ template <> double2 *vec<double>(Workspace *ws, int i) { return ws->d[i]; }
 template <typename R> static typename CT<R>::C *wvec(Workspace *ws);
 template <> float2 *wvec<float>(Workspace *ws) { return ws->w32; }
 template <> double2 *wvec<double>(Workspace *ws) { return ws->w64; }
+template <typename R> static typename CT<R>::C *jvec(Workspace *ws);
+template <> float2 *jvec<float>(Workspace *ws) { return ws->dj32; }
+template <> double2 *jvec<double>(Workspace *ws) { return ws->dj64; }
 
 static int read_scalars(fdfd_handle *h, const KScalars *dev, KScalars *host) {
   TRY(cuda_check(h, cudaMemcpyAsync(host, dev, sizeof(KScalars), cudaMemcpyDeviceToHost, h->stream), "read scalars"));
@@ -175,17 +190,30 @@ static int bicg_iter(fdfd_handle *h, Workspace *ws, bool tr) {
   return FDFD_OK;
 }
 
-// One COCG iteration on the S-symmetric operator (1 application):
-//   q = A p ; α = ρ/(pᵀ S q) ; x += α p ; r −= α q ; ρ' = rᵀ S r ; β = ρ'/ρ ; p = r + β p
+// One Jacobi-preconditioned COCG iteration on the S-symmetric operator
+// (1 application, 3 kernels), z = D⁻¹ r with D = diag(A):
+//   q = A p and pᵀ S q (fused) ; α = ρ/(pᵀ S q) ; x += α p ; r −= α q ;
+//   ρ' = rᵀ S z ; β = ρ'/ρ ; p = z + β p
 template <typename R>
 static int cocg_iter(fdfd_handle *h, Workspace *ws, bool tr) {
   using C = typename CT<R>::C;
   const long long n = ws->n;
   C *xi = vec<R>(ws, 0), *r = vec<R>(ws, 1), *p = vec<R>(ws, 2), *q = vec<R>(ws, 3);
-  TRY(launch_apply_fin<R>(h, p, q, EPI_STORE, nullptr, FIN_NONE, ws->sc, tr));
-  TRY(dot_u<R>(h, p, q, wvec<R>(ws), n, FIN_COCG_A, ws->sc));
-  TRY(cocg_xr<R>(h, xi, p, q, r, wvec<R>(ws), n, ws->sc));
-  TRY(cocg_p<R>(h, r, p, n, ws->sc));
+  TRY(launch_apply_fin<R>(h, p, q, EPI_DOT_SU, nullptr, FIN_COCG_A, ws->sc, tr));
+  TRY(cocg_xr<R>(h, xi, p, q, r, wvec<R>(ws), jvec<R>(ws), n, ws->sc));
+  TRY(cocg_p<R>(h, r, jvec<R>(ws), p, n, ws->sc));
+  return FDFD_OK;
+}
+
+// ρ = rᵀ S D⁻¹ r of the current residual (q is used as scratch for D⁻¹ r)
+template <typename R>
+static int cocg_rho(fdfd_handle *h, Workspace *ws, double2 *rho) {
+  const long long n = ws->n;
+  TRY(vmul<R>(h, vec<R>(ws, 3), jvec<R>(ws), vec<R>(ws, 1), n));
+  TRY(dot_u<R>(h, vec<R>(ws, 1), vec<R>(ws, 3), wvec<R>(ws), n, FIN_NONE, ws->scu));
+  KScalars tmp;
+  TRY(read_scalars(h, ws->scu, &tmp));
+  *rho = tmp.dot0;
   return FDFD_OK;
 }
 
@@ -239,12 +267,9 @@ static int init_inner(fdfd_handle *h, Workspace *ws, int method, double rr, KSca
   else TRY(copy<double>(h, r, ws->r64, n));
   TRY(cuda_check(h, cudaMemsetAsync(vec<R>(ws, 0), 0, bytes, h->stream), "memset x"));
   if (method == FDFD_COCG) {
-    // p = r ; ρ = rᵀ S r
-    TRY(copy<R>(h, vec<R>(ws, 2), r, n));
-    TRY(dot_u<R>(h, r, r, wvec<R>(ws), n, FIN_NONE, ws->scu));
-    KScalars tmp;
-    TRY(read_scalars(h, ws->scu, &tmp));
-    hs->rho = tmp.dot0;
+    // p = z = D⁻¹ r ; ρ = rᵀ S z
+    TRY(vmul<R>(h, vec<R>(ws, 2), jvec<R>(ws), r, n));
+    TRY(cocg_rho<R>(h, ws, &hs->rho));
   } else {
     TRY(copy<R>(h, vec<R>(ws, 2), r, n));  // r̂ = r₀
     TRY(cuda_check(h, cudaMemsetAsync(vec<R>(ws, 3), 0, bytes, h->stream), "memset p"));
@@ -334,11 +359,8 @@ static int solve_impl(fdfd_handle *h, const double2 *b, double2 *x, const fdfd_s
           hs.done = 0;
           hs.reason = 0;
           if (o.method == FDFD_COCG) {
-            // COCG's ρ = rᵀ S r must describe the replaced residual
-            TRY(dot_u<R>(h, r, r, wvec<R>(ws), n, FIN_NONE, ws->scu));
-            KScalars t2;
-            TRY(read_scalars(h, ws->scu, &t2));
-            hs.rho = t2.dot0;
+            // COCG's ρ = rᵀ S D⁻¹ r must describe the replaced residual
+            TRY(cocg_rho<R>(h, ws, &hs.rho));
           }
         }
         TRY(write_scalars(h, ws->sc, &hs));
@@ -359,6 +381,7 @@ static int solve_impl(fdfd_handle *h, const double2 *b, double2 *x, const fdfd_s
                  "copy x"));
   TRY(cuda_check(h, cudaEventRecord(h->ev1, h->stream), "event"));
   TRY(cuda_check(h, cudaEventSynchronize(h->ev1), "event sync"));
+  TRY(check_dev_err(h));
   float ms = 0.f;
   cudaEventElapsedTime(&ms, h->ev0, h->ev1);
   st.iterations = iters;

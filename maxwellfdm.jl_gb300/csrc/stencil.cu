@@ -6,17 +6,26 @@
 //
 // Kernel design (sm_103a, HBM-bound):
 //   * a CTA owns a 32×8 (x,y) tile and marches along z over a chunk of
-//     planes; a 3-slot ring of E planes (with a one-cell halo) lives in
-//     shared memory, so every E value is read from HBM about once;
-//   * H = Cₑ E is computed once per plane for the tile plus its low halo
-//     and kept for two planes (H(k-1), H(k)) in shared memory;
-//   * the output y(k) = Cₘ H − ω² Pε E is formed from shared memory with
-//     the per-axis 1/s∆l PML factors, the ε diagonal and — only where the
-//     (tile, plane) flag says so — the corner-averaged off-diagonal ε terms;
+//     planes with a ring of E planes (one-cell halo) in shared memory, so
+//     every E value is read from HBM about once;
+//   * k_apply_tma (PEC walls, Aᵀ excluded): a 4-slot ring filled by TMA
+//     (cp.async.bulk.tensor.3d, one elected thread, mbarrier completion with
+//     bounded waits), two planes ahead of the plane being computed; the
+//     out-of-bounds zero fill of TMA realises the PEC ghost planes;
+//   * k_apply (general: Bloch phases, Aᵀ): a 3-slot ring filled by plain
+//     loads that apply the boundary rules element by element;
+//   * H = Cₑ E is computed once per plane for the tile plus its low halo and
+//     kept for two planes (H(k−1), H(k)) in shared memory;
+//   * y(k) = Cₘ H − ω² Pε E is formed from shared memory with the per-axis
+//     1/s∆l PML factors, the ε diagonal and — only where the (tile, plane)
+//     flag says so — the corner-averaged off-diagonal ε terms;
 //   * optional fused epilogues produce the dot products a Krylov step needs
 //     (block partials in FP64, last-block finalisation, krylov_fin.cuh);
 //   * TRANSPOSE applies Aᵀ = S·A·S⁻¹ with S = V_E (the dual volume of each
 //     E sample), which holds because S·A is complex symmetric.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "krylov_fin.cuh"
 
 namespace fdfd {
@@ -25,12 +34,59 @@ constexpr int EX = TX + 2, EY = TY + 2;  // E tile with halo: −1 … T
 constexpr int HX = TX + 1, HY = TY + 1;  // H tile: −1 … T−1
 
 template <typename R>
-struct StencilSmem {
+struct HTile {
   using C = typename CT<R>::C;
-  C e[3][3][EY][EX];  // [slot][component][jj+1][ii+1]
   C hx[2][HY][HX];
   C hy[2][HY][HX];
   C hz[HY][HX];
+};
+
+// Per-tile copies of the x and y coefficient arrays, indexed by position+1
+// over −1 … T (ghost entries resolved by cidx).
+template <typename R>
+struct CoefTile {
+  using C = typename CT<R>::C;
+  C cmx[TX + 2], cex[TX + 2], wmx[TX + 2], wpx[TX + 2];
+  C cmy[TY + 2], cey[TY + 2], wmy[TY + 2], wpy[TY + 2];
+};
+
+// ---- plain-load ring: SoA by component, 3 slots
+template <typename R>
+struct PlainE {
+  using C = typename CT<R>::C;
+  C e[3][3][EY][EX];
+  __device__ __forceinline__ C get(int s, int c, int jj, int ii) const { return e[s][c][jj + 1][ii + 1]; }
+};
+template <typename R>
+struct PlainSmem {
+  PlainE<R> E;
+  HTile<R> H;
+  CoefTile<R> T;
+};
+
+// ---- TMA ring: the global AoS cell layout, 4 slots.  The box starts XOFF
+// cells left of the tile so its x coordinate is 16-byte aligned.
+template <typename R>
+struct TmaGeom {
+  static constexpr int XOFF = sizeof(R) == 4 ? 2 : 1;
+  static constexpr int XW = sizeof(R) == 4 ? TX + 4 : TX + 2;
+  static constexpr int NSLOT = 4;
+  static constexpr int PLANE_BYTES = XW * EY * 3 * 2 * (int)sizeof(R);
+  static constexpr int SLOT_BYTES = (PLANE_BYTES + 127) / 128 * 128;
+  static constexpr int H_OFF = NSLOT * SLOT_BYTES;
+  static constexpr int T_OFF = H_OFF + (int)((sizeof(HTile<R>) + 15) / 16 * 16);
+  static constexpr int BAR_OFF = T_OFF + (int)((sizeof(CoefTile<R>) + 15) / 16 * 16);
+  static constexpr int SMEM = BAR_OFF + NSLOT * 8 + 128;  // + alignment slack
+};
+template <typename R>
+struct TmaE {
+  using C = typename CT<R>::C;
+  unsigned char *base;
+  __device__ __forceinline__ C *ptr(int s, int c, int jj, int ii) const {
+    return reinterpret_cast<C *>(base + s * TmaGeom<R>::SLOT_BYTES) +
+           ((jj + 1) * TmaGeom<R>::XW + ii + TmaGeom<R>::XOFF) * 3 + c;
+  }
+  __device__ __forceinline__ C get(int s, int c, int jj, int ii) const { return *ptr(s, c, jj, ii); }
 };
 
 template <typename R>
@@ -106,33 +162,51 @@ __device__ __forceinline__ int cidx(const OpArgs<R> &a, int v, int g) {
 }
 
 template <typename R, bool TRANSPOSE>
-__device__ __forceinline__ void load_plane(StencilSmem<R> &S, const OpArgs<R> &a, const Extra<R> &ex,
+__device__ __forceinline__ void load_plane(PlainE<R> &E, const OpArgs<R> &a, const Extra<R> &ex,
                                            const typename CT<R>::C *__restrict__ x, int i0, int j0, int k, int slot,
                                            int tid) {
   for (int p = tid; p < EX * EY; p += NTHR) {
     const int ii = p % EX - 1, jj = p / EX - 1;
     const int gi = i0 + ii, gj = j0 + jj;
 #pragma unroll
-    for (int c = 0; c < 3; ++c) S.e[slot][c][jj + 1][ii + 1] = load_e<R, TRANSPOSE>(x, a, ex, gi, gj, k, c);
+    for (int c = 0; c < 3; ++c) E.e[slot][c][jj + 1][ii + 1] = load_e<R, TRANSPOSE>(x, a, ex, gi, gj, k, c);
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ void fill_coef(CoefTile<R> &T, const OpArgs<R> &a, int i0, int j0, int tid) {
+  if (tid < TX + 2) {
+    const int c = cidx(a, 0, i0 + tid - 1);
+    T.cmx[tid] = a.cm[0][c];
+    T.cex[tid] = a.ce[0][c];
+    T.wmx[tid] = a.wm[0][c];
+    T.wpx[tid] = a.wp[0][c];
+  } else if (tid >= 64 && tid < 64 + TY + 2) {
+    const int t = tid - 64;
+    const int c = cidx(a, 1, j0 + t - 1);
+    T.cmy[t] = a.cm[1][c];
+    T.cey[t] = a.ce[1][c];
+    T.wmy[t] = a.wm[1][c];
+    T.wpy[t] = a.wp[1][c];
   }
 }
 
 // H(k) = Cₑ E over the tile positions −1 … T−1 in x and y.
-template <typename R>
-__device__ __forceinline__ void compute_h(StencilSmem<R> &S, const OpArgs<R> &a, int i0, int j0, int k, int sk,
-                                          int sk1, int hslot, int tid) {
+template <typename R, typename ET>
+__device__ __forceinline__ void compute_h(const ET &E, HTile<R> &H, const CoefTile<R> &T, const OpArgs<R> &a,
+                                          int k, int sk, int sk1, int hslot, int tid) {
   using C = typename CT<R>::C;
   const C cmz = a.cm[2][cidx(a, 2, k)];
   for (int p = tid; p < HX * HY; p += NTHR) {
     const int ii = p % HX - 1, jj = p / HX - 1;
-    const C cmx = a.cm[0][cidx(a, 0, i0 + ii)];
-    const C cmy = a.cm[1][cidx(a, 1, j0 + jj)];
-    const C ex0 = S.e[sk][0][jj + 1][ii + 1], exy = S.e[sk][0][jj + 2][ii + 1], exz = S.e[sk1][0][jj + 1][ii + 1];
-    const C ey0 = S.e[sk][1][jj + 1][ii + 1], eyx = S.e[sk][1][jj + 1][ii + 2], eyz = S.e[sk1][1][jj + 1][ii + 1];
-    const C ez0 = S.e[sk][2][jj + 1][ii + 1], ezx = S.e[sk][2][jj + 1][ii + 2], ezy = S.e[sk][2][jj + 2][ii + 1];
-    S.hx[hslot][jj + 1][ii + 1] = csub(cmul(cmy, csub(ezy, ez0)), cmul(cmz, csub(eyz, ey0)));
-    S.hy[hslot][jj + 1][ii + 1] = csub(cmul(cmz, csub(exz, ex0)), cmul(cmx, csub(ezx, ez0)));
-    S.hz[jj + 1][ii + 1] = csub(cmul(cmx, csub(eyx, ey0)), cmul(cmy, csub(exy, ex0)));
+    const C cmx = T.cmx[ii + 1];
+    const C cmy = T.cmy[jj + 1];
+    const C ex0 = E.get(sk, 0, jj, ii), exy = E.get(sk, 0, jj + 1, ii), exz = E.get(sk1, 0, jj, ii);
+    const C ey0 = E.get(sk, 1, jj, ii), eyx = E.get(sk, 1, jj, ii + 1), eyz = E.get(sk1, 1, jj, ii);
+    const C ez0 = E.get(sk, 2, jj, ii), ezx = E.get(sk, 2, jj, ii + 1), ezy = E.get(sk, 2, jj + 1, ii);
+    H.hx[hslot][jj + 1][ii + 1] = csub(cmul(cmy, csub(ezy, ez0)), cmul(cmz, csub(eyz, ey0)));
+    H.hy[hslot][jj + 1][ii + 1] = csub(cmul(cmz, csub(exz, ex0)), cmul(cmx, csub(ezx, ez0)));
+    H.hz[jj + 1][ii + 1] = csub(cmul(cmx, csub(eyx, ey0)), cmul(cmy, csub(exy, ex0)));
   }
 }
 
@@ -145,14 +219,159 @@ __device__ __forceinline__ R ld_eoff(const OpArgs<R> &a, int p, int gi, int gj, 
   return a.eoff[(long long)p * a.ncell + gi + (long long)a.N[0] * (gj + (long long)a.N[1] * gk)];
 }
 
+template <typename R> struct Accs {
+  Acc<R> r0, i0, r1;
+};
+
+// Operands of the output stage that come from global memory, loaded at the
+// top of a plane iteration so their latency overlaps the H computation: the
+// ε diagonal and the epilogue's second operand at the thread's cell.
+template <typename R>
+struct Pre {
+  using C = typename CT<R>::C;
+  R e0, e1, e2;
+  C a0, a1, a2;
+};
+
+template <typename R, int EPI>
+__device__ __forceinline__ void prefetch(Pre<R> &pf, const OpArgs<R> &a, const typename CT<R>::C *__restrict__ aux0,
+                                         long long cell) {
+  pf.e0 = a.eps[cell];
+  pf.e1 = a.eps[a.ncell + cell];
+  pf.e2 = a.eps[2 * a.ncell + cell];
+  if (EPI == EPI_RESID || EPI == EPI_DOT_AUX) {
+    pf.a0 = aux0[3 * cell];
+    pf.a1 = aux0[3 * cell + 1];
+    pf.a2 = aux0[3 * cell + 2];
+  }
+}
+
+// y(k) at the thread's cell (gi, gj, k) from shared memory.
+template <typename R, int EPI, bool TRANSPOSE, typename ET>
+__device__ __forceinline__ void output_cell(const ET &E, const HTile<R> &H, const CoefTile<R> &T, const OpArgs<R> &a,
+                                            const Extra<R> &ex, const Pre<R> &pf,
+                                            const typename CT<R>::C *__restrict__ x,
+                                            typename CT<R>::C *__restrict__ y, int gi, int gj, int k, int tx, int ty,
+                                            int sm, int s0, int s1, int hc, int hp, bool offd, Accs<R> &acc) {
+  using C = typename CT<R>::C;
+  const C cez = a.ce[2][k];
+  const C cex = T.cex[tx + 1], cey = T.cey[ty + 1];
+  const C hz00 = H.hz[ty + 1][tx + 1], hzjm = H.hz[ty][tx + 1], hzim = H.hz[ty + 1][tx];
+  const C hyk = H.hy[hc][ty + 1][tx + 1], hykm = H.hy[hp][ty + 1][tx + 1], hyim = H.hy[hc][ty + 1][tx];
+  const C hxk = H.hx[hc][ty + 1][tx + 1], hxkm = H.hx[hp][ty + 1][tx + 1], hxjm = H.hx[hc][ty][tx + 1];
+  C yx = csub(cmul(cey, csub(hz00, hzjm)), cmul(cez, csub(hyk, hykm)));
+  C yy = csub(cmul(cez, csub(hxk, hxkm)), cmul(cex, csub(hz00, hzim)));
+  C yz = csub(cmul(cex, csub(hyk, hyim)), cmul(cey, csub(hxk, hxjm)));
+  const long long cell = gi + (long long)a.N[0] * (gj + (long long)a.N[1] * k);
+  // pinned outputs: E_c at primal index 0 along a non-Bloch axis v ≠ c
+  const bool pin_xy = !a.bloch[1] && gj == 0;
+  const bool pin_yx = !a.bloch[0] && gi == 0;
+  const bool pkz = !a.bloch[2] && k == 0;
+  const bool pinx = pin_xy || pkz;
+  const bool piny = pin_yx || pkz;
+  const bool pinz = pin_yx || pin_xy;
+  // the cell's own values: shared memory holds 0 for pinned DOFs (they do
+  // not enter the curl), but the ε term uses the true value
+  C e_x = E.get(s0, 0, ty, tx), e_y = E.get(s0, 1, ty, tx), e_z = E.get(s0, 2, ty, tx);
+  if (pinx) e_x = own_e<R, TRANSPOSE>(x, ex, cell, 0, gi, gj, k);
+  if (piny) e_y = own_e<R, TRANSPOSE>(x, ex, cell, 1, gi, gj, k);
+  if (pinz) e_z = own_e<R, TRANSPOSE>(x, ex, cell, 2, gi, gj, k);
+  C dx = cscale(e_x, pf.e0);
+  C dy = cscale(e_y, pf.e1);
+  C dz = cscale(e_z, pf.e2);
+  if (offd) {
+    const C wmz = a.wm[2][k], wpz = a.wp[2][k];
+    const C wmx = T.wmx[tx + 1], wpx = T.wpx[tx + 1], wmy = T.wmy[ty + 1], wpy = T.wpy[ty + 1];
+    C ox = czero<C>(), oy = czero<C>(), oz = czero<C>();
+    // x output: corners (i', j, k), i' ∈ {i, i+1}
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const C eym = E.get(s0, 1, ty - 1, tx + s), eyp = E.get(s0, 1, ty, tx + s);
+      const C ezm = E.get(sm, 2, ty, tx + s), ezp = E.get(s0, 2, ty, tx + s);
+      const R exy = ld_eoff(a, 0, gi + s, gj, k), ezx = ld_eoff(a, 2, gi + s, gj, k);
+      ox = cadd(ox, cscale(cadd(cmul(wmy, eym), cmul(wpy, eyp)), exy));
+      ox = cadd(ox, cscale(cadd(cmul(wmz, ezm), cmul(wpz, ezp)), ezx));
+    }
+    // y output: corners (i, j', k), j' ∈ {j, j+1}
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const C exm = E.get(s0, 0, ty + s, tx - 1), exp_ = E.get(s0, 0, ty + s, tx);
+      const C ezm = E.get(sm, 2, ty + s, tx), ezp = E.get(s0, 2, ty + s, tx);
+      const R exy = ld_eoff(a, 0, gi, gj + s, k), eyz = ld_eoff(a, 1, gi, gj + s, k);
+      oy = cadd(oy, cscale(cadd(cmul(wmx, exm), cmul(wpx, exp_)), exy));
+      oy = cadd(oy, cscale(cadd(cmul(wmz, ezm), cmul(wpz, ezp)), eyz));
+    }
+    // z output: corners (i, j, k'), k' ∈ {k, k+1}
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const int sl = s ? s1 : s0;
+      const C exm = E.get(sl, 0, ty, tx - 1), exp_ = E.get(sl, 0, ty, tx);
+      const C eym = E.get(sl, 1, ty - 1, tx), eyp = E.get(sl, 1, ty, tx);
+      const R ezx = ld_eoff(a, 2, gi, gj, k + s), eyz = ld_eoff(a, 1, gi, gj, k + s);
+      oz = cadd(oz, cscale(cadd(cmul(wmx, exm), cmul(wpx, exp_)), ezx));
+      oz = cadd(oz, cscale(cadd(cmul(wmy, eym), cmul(wpy, eyp)), eyz));
+    }
+    if (!pinx) dx = cadd(dx, cscale(ox, R(0.5)));
+    if (!piny) dy = cadd(dy, cscale(oy, R(0.5)));
+    if (!pinz) dz = cadd(dz, cscale(oz, R(0.5)));
+  }
+  if (pinx) yx = czero<C>();
+  if (piny) yy = czero<C>();
+  if (pinz) yz = czero<C>();
+  yx = csub(yx, cmul(a.w2, dx));
+  yy = csub(yy, cmul(a.w2, dy));
+  yz = csub(yz, cmul(a.w2, dz));
+  if (TRANSPOSE) {
+    yx = cmul(yx, vol_e<R>(ex, 0, gi, gj, k));
+    yy = cmul(yy, vol_e<R>(ex, 1, gi, gj, k));
+    yz = cmul(yz, vol_e<R>(ex, 2, gi, gj, k));
+  }
+  C *yo = y + 3 * cell;
+  if (EPI == EPI_RESID) {
+    yx = csub(pf.a0, yx);
+    yy = csub(pf.a1, yy);
+    yz = csub(pf.a2, yz);
+    acc.r0.add(yx.x * yx.x + yx.y * yx.y + yy.x * yy.x + yy.y * yy.y + yz.x * yz.x + yz.y * yz.y);
+  } else if (EPI == EPI_DOT_AUX) {
+    const C d0 = cdotc(pf.a0, yx), d1 = cdotc(pf.a1, yy), d2 = cdotc(pf.a2, yz);
+    acc.r0.add(d0.x + d1.x + d2.x);
+    acc.i0.add(d0.y + d1.y + d2.y);
+  } else if (EPI == EPI_DOT_TS) {
+    // (t, s) with the unscaled input s (shared memory holds S⁻¹ s for Aᵀ)
+    const C sx = TRANSPOSE ? x[3 * cell] : e_x, sy = TRANSPOSE ? x[3 * cell + 1] : e_y,
+            sz = TRANSPOSE ? x[3 * cell + 2] : e_z;
+    const C d0 = cdotc(yx, sx), d1 = cdotc(yy, sy), d2 = cdotc(yz, sz);
+    acc.r0.add(d0.x + d1.x + d2.x);
+    acc.i0.add(d0.y + d1.y + d2.y);
+    acc.r1.add(yx.x * yx.x + yx.y * yx.y + yy.x * yy.x + yy.y * yy.y + yz.x * yz.x + yz.y * yz.y);
+  } else if (EPI == EPI_DOT_SU) {
+    // Σ V_E·x·y over the cell (COCG's S-weighted bilinear form)
+    const C d0 = cmul(cmul(vol_e<R>(ex, 0, gi, gj, k), e_x), yx);
+    const C d1 = cmul(cmul(vol_e<R>(ex, 1, gi, gj, k), e_y), yy);
+    const C d2 = cmul(cmul(vol_e<R>(ex, 2, gi, gj, k), e_z), yz);
+    acc.r0.add(d0.x + d1.x + d2.x);
+    acc.i0.add(d0.y + d1.y + d2.y);
+  }
+  yo[0] = yx;
+  yo[1] = yy;
+  yo[2] = yz;
+}
+
+__device__ __forceinline__ bool offd_on(const OpArgs<float> &a, long long tilecol, int k) {
+  return a.eoff != nullptr && (a.oflag == nullptr || a.oflag[tilecol * a.N[2] + k]);
+}
+__device__ __forceinline__ bool offd_on(const OpArgs<double> &a, long long tilecol, int k) {
+  return a.eoff != nullptr && (a.oflag == nullptr || a.oflag[tilecol * a.N[2] + k]);
+}
+
+// ------------------------------------------------------------------ plain kernel
 template <typename R, int EPI, bool TRANSPOSE>
 __global__ void __launch_bounds__(NTHR) k_apply(OpArgs<R> a, Extra<R> ex, const typename CT<R>::C *__restrict__ x,
                                                 typename CT<R>::C *__restrict__ y,
                                                 const typename CT<R>::C *__restrict__ aux0, RedBuf red, int fin,
                                                 KScalars *sc) {
-  using C = typename CT<R>::C;
   extern __shared__ __align__(16) unsigned char smraw[];
-  StencilSmem<R> &S = *reinterpret_cast<StencilSmem<R> *>(smraw);
+  PlainSmem<R> &S = *reinterpret_cast<PlainSmem<R> *>(smraw);
   if (sc != nullptr && sc->done) return;
 
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
@@ -161,131 +380,177 @@ __global__ void __launch_bounds__(NTHR) k_apply(OpArgs<R> a, Extra<R> ex, const 
   const int k1 = min(k0 + ex.kchunk, a.N[2]);
   const int gi = i0 + tx, gj = j0 + ty;
   const bool active = (gi < a.N[0]) && (gj < a.N[1]);
-  const long long plane = (long long)a.N[0] * a.N[1];
   const long long tilecol = blockIdx.x + (long long)gridDim.x * blockIdx.y;
+  Accs<R> acc;
 
-  Acc<R> acc0r, acc0i, acc1r, acc1i;
-
-  // preamble: E(k0−1), E(k0), E(k0+1); H(k0−1)
-  load_plane<R, TRANSPOSE>(S, a, ex, x, i0, j0, k0 - 1, (k0 + 2) % 3, tid);
-  load_plane<R, TRANSPOSE>(S, a, ex, x, i0, j0, k0, k0 % 3, tid);
-  load_plane<R, TRANSPOSE>(S, a, ex, x, i0, j0, k0 + 1, (k0 + 1) % 3, tid);
+  // preamble: coefficient tables; E(k0−1), E(k0), E(k0+1); H(k0−1)
+  fill_coef<R>(S.T, a, i0, j0, tid);
+  load_plane<R, TRANSPOSE>(S.E, a, ex, x, i0, j0, k0 - 1, (k0 + 2) % 3, tid);
+  load_plane<R, TRANSPOSE>(S.E, a, ex, x, i0, j0, k0, k0 % 3, tid);
+  load_plane<R, TRANSPOSE>(S.E, a, ex, x, i0, j0, k0 + 1, (k0 + 1) % 3, tid);
   __syncthreads();
-  compute_h<R>(S, a, i0, j0, k0 - 1, (k0 + 2) % 3, k0 % 3, (k0 + 1) & 1, tid);
-
-  // per-thread constants
-  const int cxi = cidx(a, 0, gi), cyj = cidx(a, 1, gj);
-  const C cex = a.ce[0][cxi], cey = a.ce[1][cyj];
-  const C wmx = a.wm[0][cxi], wpx = a.wp[0][cxi], wmy = a.wm[1][cyj], wpy = a.wp[1][cyj];
-  // pinned outputs: E_c at primal index 0 along a non-Bloch axis v ≠ c
-  const bool pin_xy = !a.bloch[1] && gj == 0;
-  const bool pin_yx = !a.bloch[0] && gi == 0;
-  const bool pinz = pin_yx || pin_xy;
+  compute_h<R>(S.E, S.H, S.T, a, k0 - 1, (k0 + 2) % 3, k0 % 3, (k0 + 1) & 1, tid);
 
   for (int k = k0; k < k1; ++k) {
     const int sm = (k + 2) % 3, s0 = k % 3, s1 = (k + 1) % 3;
     const int hc = k & 1, hp = (k + 1) & 1;
+    Pre<R> pf;
+    if (active) prefetch<R, EPI>(pf, a, aux0, gi + (long long)a.N[0] * (gj + (long long)a.N[1] * k));
     __syncthreads();  // E(k+1) present, H(k−1) complete
-    compute_h<R>(S, a, i0, j0, k, s0, s1, hc, tid);
+    compute_h<R>(S.E, S.H, S.T, a, k, s0, s1, hc, tid);
     __syncthreads();
-    if (active) {
-      const C cez = a.ce[2][k];
-      const C hz00 = S.hz[ty + 1][tx + 1], hzjm = S.hz[ty][tx + 1], hzim = S.hz[ty + 1][tx];
-      const C hyk = S.hy[hc][ty + 1][tx + 1], hykm = S.hy[hp][ty + 1][tx + 1], hyim = S.hy[hc][ty + 1][tx];
-      const C hxk = S.hx[hc][ty + 1][tx + 1], hxkm = S.hx[hp][ty + 1][tx + 1], hxjm = S.hx[hc][ty][tx + 1];
-      C yx = csub(cmul(cey, csub(hz00, hzjm)), cmul(cez, csub(hyk, hykm)));
-      C yy = csub(cmul(cez, csub(hxk, hxkm)), cmul(cex, csub(hz00, hzim)));
-      C yz = csub(cmul(cex, csub(hyk, hyim)), cmul(cey, csub(hxk, hxjm)));
-      const long long cell = gi + (long long)a.N[0] * gj + plane * k;
-      const bool pkz = !a.bloch[2] && k == 0;
-      const bool pinx = pin_xy || pkz;
-      const bool piny = pin_yx || pkz;
-      // the cell's own values: shared memory holds 0 for pinned DOFs (they
-      // do not enter the curl), but the ε term uses the true value
-      C e_x = S.e[s0][0][ty + 1][tx + 1], e_y = S.e[s0][1][ty + 1][tx + 1], e_z = S.e[s0][2][ty + 1][tx + 1];
-      if (pinx) e_x = own_e<R, TRANSPOSE>(x, ex, cell, 0, gi, gj, k);
-      if (piny) e_y = own_e<R, TRANSPOSE>(x, ex, cell, 1, gi, gj, k);
-      if (pinz) e_z = own_e<R, TRANSPOSE>(x, ex, cell, 2, gi, gj, k);
-      C dx = cscale(e_x, a.eps[cell]);
-      C dy = cscale(e_y, a.eps[a.ncell + cell]);
-      C dz = cscale(e_z, a.eps[2 * a.ncell + cell]);
-      if (a.eoff != nullptr && (a.oflag == nullptr || a.oflag[tilecol * a.N[2] + k])) {
-        const C wmz = a.wm[2][k], wpz = a.wp[2][k];
-        // x output: corners (i', j, k), i' ∈ {i, i+1}
-        C ox = czero<C>(), oy = czero<C>(), oz = czero<C>();
-#pragma unroll
-        for (int s = 0; s < 2; ++s) {
-          const C eym = S.e[s0][1][ty][tx + 1 + s], eyp = S.e[s0][1][ty + 1][tx + 1 + s];
-          const C ezm = S.e[sm][2][ty + 1][tx + 1 + s], ezp = S.e[s0][2][ty + 1][tx + 1 + s];
-          const R exy = ld_eoff(a, 0, gi + s, gj, k), ezx = ld_eoff(a, 2, gi + s, gj, k);
-          ox = cadd(ox, cscale(cadd(cmul(wmy, eym), cmul(wpy, eyp)), exy));
-          ox = cadd(ox, cscale(cadd(cmul(wmz, ezm), cmul(wpz, ezp)), ezx));
-        }
-        // y output: corners (i, j', k), j' ∈ {j, j+1}
-#pragma unroll
-        for (int s = 0; s < 2; ++s) {
-          const C exm = S.e[s0][0][ty + 1 + s][tx], exp_ = S.e[s0][0][ty + 1 + s][tx + 1];
-          const C ezm = S.e[sm][2][ty + 1 + s][tx + 1], ezp = S.e[s0][2][ty + 1 + s][tx + 1];
-          const R exy = ld_eoff(a, 0, gi, gj + s, k), eyz = ld_eoff(a, 1, gi, gj + s, k);
-          oy = cadd(oy, cscale(cadd(cmul(wmx, exm), cmul(wpx, exp_)), exy));
-          oy = cadd(oy, cscale(cadd(cmul(wmz, ezm), cmul(wpz, ezp)), eyz));
-        }
-        // z output: corners (i, j, k'), k' ∈ {k, k+1}
-#pragma unroll
-        for (int s = 0; s < 2; ++s) {
-          const int sl = s ? s1 : s0;
-          const C exm = S.e[sl][0][ty + 1][tx], exp_ = S.e[sl][0][ty + 1][tx + 1];
-          const C eym = S.e[sl][1][ty][tx + 1], eyp = S.e[sl][1][ty + 1][tx + 1];
-          const R ezx = ld_eoff(a, 2, gi, gj, k + s), eyz = ld_eoff(a, 1, gi, gj, k + s);
-          oz = cadd(oz, cscale(cadd(cmul(wmx, exm), cmul(wpx, exp_)), ezx));
-          oz = cadd(oz, cscale(cadd(cmul(wmy, eym), cmul(wpy, eyp)), eyz));
-        }
-        if (!pinx) dx = cadd(dx, cscale(ox, R(0.5)));
-        if (!piny) dy = cadd(dy, cscale(oy, R(0.5)));
-        if (!pinz) dz = cadd(dz, cscale(oz, R(0.5)));
-      }
-      if (pinx) yx = czero<C>();
-      if (piny) yy = czero<C>();
-      if (pinz) yz = czero<C>();
-      yx = csub(yx, cmul(a.w2, dx));
-      yy = csub(yy, cmul(a.w2, dy));
-      yz = csub(yz, cmul(a.w2, dz));
-      if (TRANSPOSE) {
-        yx = cmul(yx, vol_e<R>(ex, 0, gi, gj, k));
-        yy = cmul(yy, vol_e<R>(ex, 1, gi, gj, k));
-        yz = cmul(yz, vol_e<R>(ex, 2, gi, gj, k));
-      }
-      C *yo = y + 3 * cell;
-      if (EPI == EPI_RESID) {
-        const C *bo = aux0 + 3 * cell;
-        yx = csub(bo[0], yx);
-        yy = csub(bo[1], yy);
-        yz = csub(bo[2], yz);
-        acc0r.add(yx.x * yx.x + yx.y * yx.y + yy.x * yy.x + yy.y * yy.y + yz.x * yz.x + yz.y * yz.y);
-      } else if (EPI == EPI_DOT_AUX) {
-        const C *ro = aux0 + 3 * cell;
-        const C d0 = cdotc(ro[0], yx), d1 = cdotc(ro[1], yy), d2 = cdotc(ro[2], yz);
-        acc0r.add(d0.x + d1.x + d2.x);
-        acc0i.add(d0.y + d1.y + d2.y);
-      } else if (EPI == EPI_DOT_TS) {
-        // (t, s) with the unscaled input s (shared memory holds S⁻¹ s for Aᵀ)
-        const C sx = TRANSPOSE ? x[3 * cell] : e_x, sy = TRANSPOSE ? x[3 * cell + 1] : e_y,
-                sz = TRANSPOSE ? x[3 * cell + 2] : e_z;
-        const C d0 = cdotc(yx, sx), d1 = cdotc(yy, sy), d2 = cdotc(yz, sz);
-        acc0r.add(d0.x + d1.x + d2.x);
-        acc0i.add(d0.y + d1.y + d2.y);
-        acc1r.add(yx.x * yx.x + yx.y * yx.y + yy.x * yy.x + yy.y * yy.y + yz.x * yz.x + yz.y * yz.y);
-      }
-      yo[0] = yx;
-      yo[1] = yy;
-      yo[2] = yz;
-    }
+    if (active)
+      output_cell<R, EPI, TRANSPOSE>(S.E, S.H, S.T, a, ex, pf, x, y, gi, gj, k, tx, ty, sm, s0, s1, hc, hp,
+                                     offd_on(a, tilecol, k), acc);
     __syncthreads();  // everyone done with E(k−1) and H(k−1)
-    if (k + 1 < k1) load_plane<R, TRANSPOSE>(S, a, ex, x, i0, j0, k + 2, sm, tid);
+    if (k + 1 < k1) load_plane<R, TRANSPOSE>(S.E, a, ex, x, i0, j0, k + 2, sm, tid);
   }
   if (EPI != EPI_STORE) {
-    block_reduce_finalise<NTHR>(make_double2(acc0r.get(), acc0i.get()), make_double2(acc1r.get(), acc1i.get()), red,
-                                fin, sc);
+    block_reduce_finalise<NTHR>(make_double2(acc.r0.get(), acc.i0.get()), make_double2(acc.r1.get(), 0.0), red, fin,
+                                sc);
+  }
+}
+
+// ------------------------------------------------------------------ TMA kernel
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void tma_load_plane(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2,
+                                               uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
+      : "memory");
+}
+// Bounded wait on an mbarrier phase: gives up after ~2^31 SM clocks (about
+// one second) and reports false instead of spinning forever.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  const long long t0 = clock64();
+  while (true) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (clock64() - t0 > (1ll << 31)) return false;
+  }
+}
+
+// Zero the pinned DOFs of a freshly landed plane (their Cₑ columns are 0):
+// E_y, E_z on x = 0; E_x, E_z on y = 0; E_x, E_y on z = 0 (PEC walls).
+template <typename R>
+__device__ __forceinline__ void pin_fixup(const TmaE<R> &E, int slot, int i0, int j0, int q, int tid) {
+  using C = typename CT<R>::C;
+  using G = TmaGeom<R>;
+  const C z = czero<C>();
+  if (q == 0) {
+    for (int p = tid; p < G::XW * EY; p += NTHR) {
+      const int ii = p % G::XW - G::XOFF, jj = p / G::XW - 1;
+      *E.ptr(slot, 0, jj, ii) = z;
+      *E.ptr(slot, 1, jj, ii) = z;
+    }
+  }
+  if (i0 == 0) {
+    for (int jj = tid - 1; jj <= TY; jj += NTHR) {
+      *E.ptr(slot, 1, jj, 0) = z;
+      *E.ptr(slot, 2, jj, 0) = z;
+    }
+  }
+  if (j0 == 0) {
+    for (int p = tid; p < G::XW; p += NTHR) {
+      const int ii = p - G::XOFF;
+      *E.ptr(slot, 0, 0, ii) = z;
+      *E.ptr(slot, 2, 0, ii) = z;
+    }
+  }
+}
+
+template <typename R, int EPI>
+__global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2) k_apply_tma(const __grid_constant__ CUtensorMap tmap, OpArgs<R> a,
+                                                    Extra<R> ex, const typename CT<R>::C *__restrict__ x,
+                                                    typename CT<R>::C *__restrict__ y,
+                                                    const typename CT<R>::C *__restrict__ aux0, RedBuf red, int fin,
+                                                    KScalars *sc, int *errflag) {
+  using G = TmaGeom<R>;
+  extern __shared__ __align__(128) unsigned char smdyn[];
+  // TMA destinations must be 128-byte aligned
+  unsigned char *smraw = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smdyn) + 127) & ~uintptr_t(127));
+  TmaE<R> E{smraw};
+  HTile<R> &H = *reinterpret_cast<HTile<R> *>(smraw + G::H_OFF);
+  CoefTile<R> &T = *reinterpret_cast<CoefTile<R> *>(smraw + G::T_OFF);
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smraw + G::BAR_OFF);
+  if (sc != nullptr && sc->done) return;
+
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+  const int k0 = blockIdx.z * ex.kchunk;
+  const int k1 = min(k0 + ex.kchunk, a.N[2]);
+  const int gi = i0 + tx, gj = j0 + ty;
+  const bool active = (gi < a.N[0]) && (gj < a.N[1]);
+  const long long tilecol = blockIdx.x + (long long)gridDim.x * blockIdx.y;
+  const int kfirst = k0 - 1;  // planes kfirst … k1 are needed
+  const int cx = 6 * (i0 - G::XOFF), cy = j0 - 1;
+  Accs<R> acc;
+  bool ok = true;
+
+  if (tid == 0) {
+    for (int s = 0; s < G::NSLOT; ++s) mbar_init(smem_u32(&bars[s]), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (tid == 0) {
+    for (int p = 0; p < G::NSLOT; ++p) {
+      const int q = kfirst + p;
+      if (q <= k1)
+        tma_load_plane(smem_u32(smraw + p * G::SLOT_BYTES), &tmap, cx, cy, q, smem_u32(&bars[p]), G::PLANE_BYTES);
+    }
+  }
+  fill_coef<R>(T, a, i0, j0, tid);
+  ok = mbar_wait(smem_u32(&bars[0]), 0) && ok;
+  ok = mbar_wait(smem_u32(&bars[1]), 0) && ok;
+  pin_fixup<R>(E, 0, i0, j0, kfirst, tid);
+  pin_fixup<R>(E, 1, i0, j0, k0, tid);
+  __syncthreads();
+  compute_h<R>(E, H, T, a, kfirst, 0, 1, (k0 + 1) & 1, tid);
+
+  for (int k = k0; k < k1; ++k) {
+    const int pm = k - 1 - kfirst, p0 = k - kfirst, p1 = k + 1 - kfirst;
+    const int sm = pm % G::NSLOT, s0 = p0 % G::NSLOT, s1 = p1 % G::NSLOT;
+    const int hc = k & 1, hp = (k + 1) & 1;
+    Pre<R> pf;
+    if (active) prefetch<R, EPI>(pf, a, aux0, gi + (long long)a.N[0] * (gj + (long long)a.N[1] * k));
+    ok = mbar_wait(smem_u32(&bars[s1]), (p1 / G::NSLOT) & 1) && ok;
+    pin_fixup<R>(E, s1, i0, j0, k + 1, tid);
+    __syncthreads();  // E(k+1) present and fixed up, H(k−1) complete
+    compute_h<R>(E, H, T, a, k, s0, s1, hc, tid);
+    __syncthreads();
+    if (active)
+      output_cell<R, EPI, false>(E, H, T, a, ex, pf, x, y, gi, gj, k, tx, ty, sm, s0, s1, hc, hp,
+                                 offd_on(a, tilecol, k), acc);
+    __syncthreads();  // slot of E(k−1) is free
+    if (tid == 0) {
+      const int q = k + 3;
+      if (q <= k1) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        tma_load_plane(smem_u32(smraw + sm * G::SLOT_BYTES), &tmap, cx, cy, q, smem_u32(&bars[sm]),
+                       G::PLANE_BYTES);
+      }
+    }
+  }
+  if (!ok) {
+    // a bounded wait gave up: report it and drain this block's copies (bounded)
+    if (tid == 0) atomicExch(errflag, 1);
+    for (int s = 0; s < G::NSLOT; ++s) mbar_wait(smem_u32(&bars[s]), 0), mbar_wait(smem_u32(&bars[s]), 1);
+  }
+  if (EPI != EPI_STORE) {
+    block_reduce_finalise<NTHR>(make_double2(acc.r0.get(), acc.i0.get()), make_double2(acc.r1.get(), 0.0), red, fin,
+                                sc);
   }
 }
 
@@ -321,9 +586,12 @@ OpArgs<R> op_args(const fdfd_handle *h) {
 template OpArgs<float> op_args<float>(const fdfd_handle *);
 template OpArgs<double> op_args<double>(const fdfd_handle *);
 
-static int kchunk_for(const fdfd_handle *h) {
+// z-chunk length (planes per CTA).  autotune_kchunk picks it per precision
+// at fdfd_create; FDFD_KCHUNK overrides; until then a heuristic aims at
+// about three resident CTAs per SM.
+static int kchunk_heuristic(const fdfd_handle *h) {
   const int tiles = ((h->N[0] + TX - 1) / TX) * ((h->N[1] + TY - 1) / TY);
-  const int target = 152 * 6;  // ~6 CTAs per SM in flight
+  const int target = 152 * 3;
   int nz = (target + tiles - 1) / tiles;
   if (nz < 1) nz = 1;
   int kc = (h->N[2] + nz - 1) / nz;
@@ -332,29 +600,26 @@ static int kchunk_for(const fdfd_handle *h) {
   return kc;
 }
 
-int apply_blocks(const fdfd_handle *h) {
-  const int kc = kchunk_for(h);
+static int kchunk_for(const fdfd_handle *h, bool c64) {
+  if (h->kc_force > 0) return h->kc_force;
+  const int t = h->kc[c64 ? 1 : 0];
+  return t > 0 ? t : kchunk_heuristic(h);
+}
+
+static int blocks_for(const fdfd_handle *h, int kc) {
   return ((h->N[0] + TX - 1) / TX) * ((h->N[1] + TY - 1) / TY) * ((h->N[2] + kc - 1) / kc);
 }
 
-template <typename R, int EPI, bool TR>
-static int launch_t(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R>::C *y,
-                    const typename CT<R>::C *aux0, int fin, KScalars *sc) {
+int apply_blocks(const fdfd_handle *h) {
+  const int a = blocks_for(h, kchunk_for(h, true)), b = blocks_for(h, kchunk_for(h, false));
+  return a > b ? a : b;
+}
+
+template <typename R>
+static Extra<R> make_extra(const fdfd_handle *h) {
   using C = typename CT<R>::C;
-  static bool attr_set[8] = {false};  // per device ordinal (≤ 8 devices per process)
-  const size_t smem = sizeof(StencilSmem<R>);
-  const int d = h->dev & 7;
-  if (!attr_set[d]) {
-    cudaError_t e = cudaFuncSetAttribute(k_apply<R, EPI, TR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return cuda_check(h, e, "cudaFuncSetAttribute(k_apply)");
-    attr_set[d] = true;
-  }
-  const int kc = kchunk_for(h);
-  dim3 grid((h->N[0] + TX - 1) / TX, (h->N[1] + TY - 1) / TY, (h->N[2] + kc - 1) / kc);
-  dim3 block(TX, TY, 1);
-  OpArgs<R> a = op_args<R>(h);
   Extra<R> ex;
-  ex.kchunk = kc;
+  ex.kchunk = kchunk_for(h, sizeof(R) == 4);
   const C *coef;
   if constexpr (sizeof(R) == 8) coef = reinterpret_cast<const C *>(h->coef64);
   else coef = reinterpret_cast<const C *>(h->coef32);
@@ -363,16 +628,160 @@ static int launch_t(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R>::
     ex.sdle[w] = coef + 4 * st + h->coef_off[w];
     ex.sdlm[w] = coef + 5 * st + h->coef_off[w];
     ex.ph[w] = mk(R(h->e_ikl[w][0]), R(h->e_ikl[w][1]));
-    double d2 = h->e_ikl[w][0] * h->e_ikl[w][0] + h->e_ikl[w][1] * h->e_ikl[w][1];
+    const double d2 = h->e_ikl[w][0] * h->e_ikl[w][0] + h->e_ikl[w][1] * h->e_ikl[w][1];
     ex.phinv[w] = mk(R(h->e_ikl[w][0] / d2), R(-h->e_ikl[w][1] / d2));
   }
+  return ex;
+}
+
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+
+// The TMA kernel serves PEC (non-Bloch) walls, the forward operator, 16-byte
+// aligned inputs and an x row pitch that is a multiple of 16 bytes.
+template <typename R>
+static bool tma_ok(const fdfd_handle *h, const void *x, bool transpose) {
+  if (transpose || h->tma_disabled) return false;
+  if (h->bloch[0] || h->bloch[1] || h->bloch[2]) return false;
+  if ((reinterpret_cast<uintptr_t>(x) & 15) != 0) return false;
+  if (((long long)h->N[0] * 6 * (long long)sizeof(R)) % 16 != 0) return false;
+  return encode_fn() != nullptr;
+}
+
+template <typename R>
+static int make_map(fdfd_handle *h, const void *x, CUtensorMap *map) {
+  using G = TmaGeom<R>;
+  const cuuint64_t dims[3] = {(cuuint64_t)6 * h->N[0], (cuuint64_t)h->N[1], (cuuint64_t)h->N[2]};
+  const cuuint64_t strides[2] = {(cuuint64_t)6 * h->N[0] * sizeof(R), (cuuint64_t)6 * h->N[0] * h->N[1] * sizeof(R)};
+  const cuuint32_t box[3] = {(cuuint32_t)(6 * G::XW), (cuuint32_t)EY, 1u};
+  const cuuint32_t estr[3] = {1u, 1u, 1u};
+  CUresult r = encode_fn()(map, sizeof(R) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3,
+                           const_cast<void *>(x), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                           CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_error(h, FDFD_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+  return FDFD_OK;
+}
+
+template <typename R, int EPI, bool TR>
+static int launch_t(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R>::C *y,
+                    const typename CT<R>::C *aux0, int fin, KScalars *sc) {
+  const Extra<R> ex = make_extra<R>(h);
+  dim3 grid((h->N[0] + TX - 1) / TX, (h->N[1] + TY - 1) / TY, (h->N[2] + ex.kchunk - 1) / ex.kchunk);
+  dim3 block(TX, TY, 1);
+  const OpArgs<R> a = op_args<R>(h);
   if (EPI != EPI_STORE) {
     int rc = ensure_red(h, (int)(grid.x * grid.y * grid.z));
     if (rc) return rc;
   }
+  const int d = h->dev & 7;
+  if (!TR && tma_ok<R>(h, x, TR)) {
+    static bool attr_tma[8] = {false};
+    const int smem = TmaGeom<R>::SMEM;
+    if (!attr_tma[d]) {
+      cudaError_t e = cudaFuncSetAttribute(k_apply_tma<R, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+      if (e != cudaSuccess) return cuda_check(h, e, "cudaFuncSetAttribute(k_apply_tma)");
+      // shared memory, not L1, limits how many CTAs fit on an SM
+      e = cudaFuncSetAttribute(k_apply_tma<R, EPI>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               cudaSharedmemCarveoutMaxShared);
+      if (e != cudaSuccess) return cuda_check(h, e, "cudaFuncSetAttribute(carveout)");
+      attr_tma[d] = true;
+    }
+    CUtensorMap map;
+    int rc = make_map<R>(h, x, &map);
+    if (rc) return rc;
+    k_apply_tma<R, EPI><<<grid, block, smem, h->stream>>>(map, a, ex, x, y, aux0, h->red, fin, sc, h->dev_err);
+    h->launches++;
+    return cuda_check(h, cudaGetLastError(), "k_apply_tma launch");
+  }
+  static bool attr_set[8] = {false};  // per device ordinal (≤ 8 devices per process)
+  const size_t smem = sizeof(PlainSmem<R>);
+  if (!attr_set[d]) {
+    cudaError_t e = cudaFuncSetAttribute(k_apply<R, EPI, TR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_check(h, e, "cudaFuncSetAttribute(k_apply)");
+    attr_set[d] = true;
+  }
   k_apply<R, EPI, TR><<<grid, block, smem, h->stream>>>(a, ex, x, y, aux0, h->red, fin, sc);
   h->launches++;
   return cuda_check(h, cudaGetLastError(), "k_apply launch");
+}
+
+// Autotuner for the z-chunk length: times y = A x for each candidate with
+// CUDA events on the handle's stream — one warm-up, then three launches each
+// preceded by an L2 flush (a 192 MiB memset, larger than the 129 MB L2), so
+// the choice holds for inputs streamed from HBM — and keeps the fastest,
+// separately for complex64 and complex128.  Runs once at fdfd_create, before
+// any solve is captured into a CUDA graph.
+int autotune_kchunk(fdfd_handle *h) {
+  if (h->kc_force > 0) return FDFD_OK;
+  const size_t n = 3 * (size_t)h->ncell;
+  const size_t flush_bytes = 192ull << 20;
+  void *bx = nullptr, *by = nullptr, *fl = nullptr;
+  if (cudaMalloc(&bx, n * sizeof(double2)) != cudaSuccess || cudaMalloc(&by, n * sizeof(double2)) != cudaSuccess ||
+      cudaMalloc(&fl, flush_bytes) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(bx);
+    cudaFree(by);
+    return set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(autotune buffers) failed");
+  }
+  int rc = cuda_check(h, cudaMemsetAsync(bx, 0, n * sizeof(double2), h->stream), "memset");
+  const int cand[] = {4, 6, 8, 12, 16, 24, 32, 48, 64};
+  const bool verbose = std::getenv("FDFD_VERBOSE") != nullptr;
+  for (int prec = 0; prec < 2 && rc == FDFD_OK; ++prec) {
+    float best = 1e30f;
+    int best_kc = 0, last_chunks = -1;
+    for (int kc : cand) {
+      if (kc > h->N[2] && last_chunks == 1) break;
+      const int chunks = (h->N[2] + kc - 1) / kc;
+      if (chunks == last_chunks) continue;
+      last_chunks = chunks;
+      h->kc[prec] = kc;
+      auto launch = [&]() {
+        return prec == 1 ? launch_apply_fin<float>(h, (const float2 *)bx, (float2 *)by, EPI_STORE, nullptr, FIN_NONE,
+                                                   nullptr, false)
+                         : launch_apply_fin<double>(h, (const double2 *)bx, (double2 *)by, EPI_STORE, nullptr,
+                                                    FIN_NONE, nullptr, false);
+      };
+      if ((rc = launch())) break;
+      float total = 0.f;
+      for (int r = 0; r < 3 && rc == FDFD_OK; ++r) {
+        cudaMemsetAsync(fl, r, flush_bytes, h->stream);
+        cudaEventRecord(h->ev0, h->stream);
+        rc = launch();
+        cudaEventRecord(h->ev1, h->stream);
+        if (rc || (rc = cuda_check(h, cudaEventSynchronize(h->ev1), "autotune sync"))) break;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+        total += ms;
+      }
+      if (rc) break;
+      if (verbose) fprintf(stderr, "fdfd autotune: %s kchunk %d: %.1f us\n", prec ? "c64" : "c128", kc, total / 3 * 1e3);
+      if (total < best) {
+        best = total;
+        best_kc = kc;
+      }
+    }
+    h->kc[prec] = best_kc;
+  }
+  cudaFree(bx);
+  cudaFree(by);
+  cudaFree(fl);
+  h->launches = 0;
+  if (rc == FDFD_OK) rc = check_dev_err(h);
+  return rc;
 }
 
 // FP64 residual launcher whose block partials, arrival counter and
@@ -381,26 +790,15 @@ static int launch_t(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R>::
 // `max_blocks` partial slots.
 int launch_residual_ext(fdfd_handle *h, const double2 *x, double2 *r, const double2 *b, RedBuf red, int max_blocks,
                         KScalars *sc) {
-  const size_t smem = sizeof(StencilSmem<double>);
+  const size_t smem = sizeof(PlainSmem<double>);
   cudaError_t e =
       cudaFuncSetAttribute(k_apply<double, EPI_RESID, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_check(h, e, "cudaFuncSetAttribute(k_apply)");
-  const int kc = kchunk_for(h);
-  dim3 grid((h->N[0] + TX - 1) / TX, (h->N[1] + TY - 1) / TY, (h->N[2] + kc - 1) / kc);
+  const Extra<double> ex = make_extra<double>(h);
+  dim3 grid((h->N[0] + TX - 1) / TX, (h->N[1] + TY - 1) / TY, (h->N[2] + ex.kchunk - 1) / ex.kchunk);
   if ((long long)grid.x * grid.y * grid.z > max_blocks)
     return set_error(h, FDFD_ERR_ARG, "grid needs more thread blocks than the fixed reduction scratch holds");
-  OpArgs<double> a = op_args<double>(h);
-  Extra<double> ex;
-  ex.kchunk = kc;
-  const double2 *coef = h->coef64;
-  const int st = h->coef_stride;
-  for (int w = 0; w < 3; ++w) {
-    ex.sdle[w] = coef + 4 * st + h->coef_off[w];
-    ex.sdlm[w] = coef + 5 * st + h->coef_off[w];
-    ex.ph[w] = make_double2(h->e_ikl[w][0], h->e_ikl[w][1]);
-    const double d2 = h->e_ikl[w][0] * h->e_ikl[w][0] + h->e_ikl[w][1] * h->e_ikl[w][1];
-    ex.phinv[w] = make_double2(h->e_ikl[w][0] / d2, -h->e_ikl[w][1] / d2);
-  }
+  const OpArgs<double> a = op_args<double>(h);
   k_apply<double, EPI_RESID, false><<<grid, dim3(TX, TY, 1), smem, h->stream>>>(a, ex, x, r, b, red, FIN_NONE, sc);
   h->launches++;
   return cuda_check(h, cudaGetLastError(), "k_apply launch");
@@ -423,6 +821,7 @@ int launch_apply_fin(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R>:
       case EPI_RESID: return launch_t<R, EPI_RESID, false>(h, x, y, aux0, fin, sc);
       case EPI_DOT_AUX: return launch_t<R, EPI_DOT_AUX, false>(h, x, y, aux0, fin, sc);
       case EPI_DOT_TS: return launch_t<R, EPI_DOT_TS, false>(h, x, y, aux0, fin, sc);
+      case EPI_DOT_SU: return launch_t<R, EPI_DOT_SU, false>(h, x, y, aux0, fin, sc);
     }
   }
   return set_error(h, FDFD_ERR_ARG, "bad epilogue kind");

@@ -90,14 +90,16 @@ def test_transpose_parity(pkg, oracle, kind):
     A.close()
 
 
-def test_random_tensor_everywhere(pkg, oracle):
-    """Arbitrary ε diagonal and off-diagonal on every cell (walls included)."""
+@pytest.mark.parametrize("N", [(11, 9, 12), (12, 9, 12), (66, 17, 20)])
+def test_random_tensor_everywhere(pkg, oracle, N):
+    """Arbitrary ε diagonal and off-diagonal on every cell (walls included).
+    Odd Nx runs the plain-load kernel, even Nx the TMA kernel."""
     O = oracle
-    g = O.uniform_grid((11, 9, 12))
+    g = O.uniform_grid(N)
     sdl_e, sdl_m = O.stretched_dl(g, 2 * np.pi / 6, ((2, 3, 1), (2, 1, 3)))
     rng = np.random.default_rng(3)
-    ed = rng.uniform(1.0, 12.0, (11, 9, 12, 3))
-    eo = rng.uniform(-2.0, 2.0, (11, 9, 12, 3))
+    ed = rng.uniform(1.0, 12.0, N + (3,))
+    eo = rng.uniform(-2.0, 2.0, N + (3,))
     Ce, Cm = O.create_curls(g, sdl_e, sdl_m)
     P = O.create_paramop(g, ed, eo, sdl_e, sdl_m)
     om = 2 * np.pi / 6
@@ -168,3 +170,18 @@ def test_residual_dev(pkg, oracle):
     assert np.linalg.norm(r - r_ref) / np.linalg.norm(r_ref) < TOL64
     assert abs(rr - np.vdot(r_ref, r_ref).real) / np.vdot(r_ref, r_ref).real < 1e-12
     A.close()
+
+
+@pytest.mark.parametrize("kind", ["vacuum8", "chunks"])
+def test_tma_and_plain_kernels_agree(pkg, oracle, kind, monkeypatch):
+    """The TMA-fed kernel (PEC walls, even Nx) and the plain-load kernel run
+    the same arithmetic: outputs are bitwise equal in both precisions."""
+    S, _ = _case(oracle, kind)
+    A1 = _make_op(pkg, S)
+    monkeypatch.setenv("FDFD_DISABLE_TMA", "1")
+    A2 = _make_op(pkg, S)
+    x = _rand(A1.n, 31)
+    assert np.array_equal(A1 @ x, A2 @ x)
+    assert np.array_equal(A1.matvec(x, "c64"), A2.matvec(x, "c64"))
+    A1.close()
+    A2.close()

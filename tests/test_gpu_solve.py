@@ -97,10 +97,11 @@ def test_graph_and_plain_agree(pkg, sysx):
     A.close()
 
 
-def test_mixed_cocg_rejected(pkg, sysx):
+def test_unsupported_cocg_forms_rejected(pkg, sysx):
     S, b, _ = sysx
     A = _op(pkg, S)
-    with pytest.raises(pkg.FDFDError) as ei:
-        A.solve(b, precision="mixed", method="cocg")
-    assert ei.value.code == 2
+    for kw in ({"precision": "fp64", "transpose": True}, {"precision": "mixed"}):
+        with pytest.raises(pkg.FDFDError) as ei:
+            A.solve(b, method="cocg", **kw)
+        assert ei.value.code == 2
     A.close()
