@@ -317,7 +317,9 @@ def run_ours(args):
             "cells_per_s_c64": A.ncell / t_mv,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "traffic": _recorded_traffic(),
-                         "kernel": "k_apply<float> (A x, complex64)", "alg_bytes_per_launch": alg64,
+                         "kernel": "k_apply_tma<float, EPI_STORE> (y = A x, complex64)",
+                         "alg_bytes_per_launch": alg64,
+                         "traffic_source": "profiles/stencil_c64_96cube.md (ncu, same workload, one launch)",
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s"},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 16 * n},

@@ -36,18 +36,55 @@ __device__ __forceinline__ typename CT<R>::C tocr(double2 v) {
   return mk(R(v.x), R(v.y));
 }
 
+// Two consecutive complex elements (2q, 2q+1) per access: one 16-byte
+// float4 for complex64, two 16-byte double2 for complex128.
+__device__ __forceinline__ void ld2(const float2 *__restrict__ a, long long q, float2 &e0, float2 &e1) {
+  const float4 v = reinterpret_cast<const float4 *>(a)[q];
+  e0 = make_float2(v.x, v.y);
+  e1 = make_float2(v.z, v.w);
+}
+__device__ __forceinline__ void ld2(const double2 *__restrict__ a, long long q, double2 &e0, double2 &e1) {
+  e0 = a[2 * q];
+  e1 = a[2 * q + 1];
+}
+__device__ __forceinline__ void st2(float2 *a, long long q, float2 e0, float2 e1) {
+  reinterpret_cast<float4 *>(a)[q] = make_float4(e0.x, e0.y, e1.x, e1.y);
+}
+__device__ __forceinline__ void st2(double2 *a, long long q, double2 e0, double2 e1) {
+  a[2 * q] = e0;
+  a[2 * q + 1] = e1;
+}
+
+// Visit element pairs with a grid-stride loop; an odd last element is
+// handled by one thread.
+template <typename F2, typename F1>
+__device__ __forceinline__ void pair_loop(long long n, F2 f2, F1 f1) {
+  const long long np = n >> 1;
+  for (long long q = blockIdx.x * (long long)VB + threadIdx.x; q < np; q += (long long)gridDim.x * VB) f2(q);
+  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) f1(n - 1);
+}
+
 // p = r + β (p − ω v)
 template <typename R>
 __global__ void __launch_bounds__(VB) k_bicg_p(const typename CT<R>::C *__restrict__ r, typename CT<R>::C *p,
                                                const typename CT<R>::C *__restrict__ v, long long n,
                                                const KScalars *sc) {
   using C = typename CT<R>::C;
+  pdl_trigger();
+  pdl_wait();
   if (sc->done) return;
   const C be = tocr<R>(sc->beta), om = tocr<R>(sc->omega);
-  for (long long i = blockIdx.x * (long long)VB + threadIdx.x; i < n; i += (long long)gridDim.x * VB) {
-    const C t = csub(p[i], cmul(om, v[i]));
-    p[i] = cadd(r[i], cmul(be, t));
-  }
+  auto one = [&](C ri, C pi, C vi) { return cadd(ri, cmul(be, csub(pi, cmul(om, vi)))); };
+  pair_loop(
+      n,
+      [&](long long q) {
+        C r0, r1, p0, p1, v0, v1;
+        ld2(r, q, r0, r1);
+        ld2(p, q, p0, p1);
+        ld2(v, q, v0, v1);
+        st2(p, q, one(r0, p0, v0), one(r1, p1, v1));
+      },
+      [&](long long i) { p[i] = one(r[i], p[i], v[i]); });
 }
 
 // s = r − α v
@@ -56,10 +93,19 @@ __global__ void __launch_bounds__(VB) k_bicg_s(const typename CT<R>::C *__restri
                                                const typename CT<R>::C *__restrict__ v, typename CT<R>::C *s,
                                                long long n, const KScalars *sc) {
   using C = typename CT<R>::C;
+  pdl_trigger();
+  pdl_wait();
   if (sc->done) return;
   const C al = tocr<R>(sc->alpha);
-  for (long long i = blockIdx.x * (long long)VB + threadIdx.x; i < n; i += (long long)gridDim.x * VB)
-    s[i] = csub(r[i], cmul(al, v[i]));
+  pair_loop(
+      n,
+      [&](long long q) {
+        C r0, r1, v0, v1;
+        ld2(r, q, r0, r1);
+        ld2(v, q, v0, v1);
+        st2(s, q, csub(r0, cmul(al, v0)), csub(r1, cmul(al, v1)));
+      },
+      [&](long long i) { s[i] = csub(r[i], cmul(al, v[i])); });
 }
 
 // x += α p + ω s;  r = s − ω t;  (r̂, r), ‖r‖²  → FIN_XR
@@ -70,19 +116,39 @@ __global__ void __launch_bounds__(VB) k_bicg_xr(typename CT<R>::C *x, const type
                                                 const typename CT<R>::C *__restrict__ rh, long long n, RedBuf red,
                                                 KScalars *sc) {
   using C = typename CT<R>::C;
+  pdl_trigger();
+  pdl_wait();
   if (sc->done) return;
   const C al = tocr<R>(sc->alpha), om = tocr<R>(sc->omega);
   Acc<R> a0r, a0i, a1;
-  for (long long i = blockIdx.x * (long long)VB + threadIdx.x; i < n; i += (long long)gridDim.x * VB) {
-    const C si = s[i];
-    x[i] = cadd(x[i], cadd(cmul(al, p[i]), cmul(om, si)));
-    const C ri = csub(si, cmul(om, t[i]));
-    r[i] = ri;
-    const C d = cdotc(rh[i], ri);
+  auto acc = [&](C rhi, C ri) {
+    const C d = cdotc(rhi, ri);
     a0r.add(d.x);
     a0i.add(d.y);
     a1.add(ri.x * ri.x + ri.y * ri.y);
-  }
+  };
+  pair_loop(
+      n,
+      [&](long long q) {
+        C x0, x1, p0, p1, s0, s1, t0, t1, h0, h1;
+        ld2(s, q, s0, s1);
+        ld2(t, q, t0, t1);
+        ld2(x, q, x0, x1);
+        ld2(p, q, p0, p1);
+        ld2(rh, q, h0, h1);
+        st2(x, q, cadd(x0, cadd(cmul(al, p0), cmul(om, s0))), cadd(x1, cadd(cmul(al, p1), cmul(om, s1))));
+        const C r0 = csub(s0, cmul(om, t0)), r1 = csub(s1, cmul(om, t1));
+        st2(r, q, r0, r1);
+        acc(h0, r0);
+        acc(h1, r1);
+      },
+      [&](long long i) {
+        const C si = s[i];
+        x[i] = cadd(x[i], cadd(cmul(al, p[i]), cmul(om, si)));
+        const C ri = csub(si, cmul(om, t[i]));
+        r[i] = ri;
+        acc(rh[i], ri);
+      });
   block_reduce_finalise<VB>(make_double2(a0r.get(), a0i.get()), make_double2(a1.get(), 0.0), red, FIN_XR, sc);
 }
 
@@ -226,25 +292,25 @@ static inline int vgrid(long long n) {
 template <typename R>
 int bicg_p(fdfd_handle *h, const typename CT<R>::C *r, typename CT<R>::C *p, const typename CT<R>::C *v, long long n,
            const KScalars *sc) {
-  k_bicg_p<R><<<vgrid(n), VB, 0, h->stream>>>(r, p, v, n, sc);
+  const cudaError_t e = launch_k(h, k_bicg_p<R>, dim3(vgrid(n)), dim3(VB), 0, r, p, v, n, sc);
   h->launches++;
-  return cuda_check(h, cudaGetLastError(), "k_bicg_p");
+  return cuda_check(h, e, "k_bicg_p");
 }
 template <typename R>
 int bicg_s(fdfd_handle *h, const typename CT<R>::C *r, const typename CT<R>::C *v, typename CT<R>::C *s, long long n,
            const KScalars *sc) {
-  k_bicg_s<R><<<vgrid(n), VB, 0, h->stream>>>(r, v, s, n, sc);
+  const cudaError_t e = launch_k(h, k_bicg_s<R>, dim3(vgrid(n)), dim3(VB), 0, r, v, s, n, sc);
   h->launches++;
-  return cuda_check(h, cudaGetLastError(), "k_bicg_s");
+  return cuda_check(h, e, "k_bicg_s");
 }
 template <typename R>
 int bicg_xr(fdfd_handle *h, typename CT<R>::C *x, const typename CT<R>::C *p, const typename CT<R>::C *s,
             const typename CT<R>::C *t, typename CT<R>::C *r, const typename CT<R>::C *rh, long long n, KScalars *sc) {
   int rc = ensure_red(h, RED_BLOCKS);
   if (rc) return rc;
-  k_bicg_xr<R><<<vgrid(n), VB, 0, h->stream>>>(x, p, s, t, r, rh, n, h->red, sc);
+  const cudaError_t e = launch_k(h, k_bicg_xr<R>, dim3(vgrid(n)), dim3(VB), 0, x, p, s, t, r, rh, n, h->red, sc);
   h->launches++;
-  return cuda_check(h, cudaGetLastError(), "k_bicg_xr");
+  return cuda_check(h, e, "k_bicg_xr");
 }
 template <typename R>
 int cocg_xr(fdfd_handle *h, typename CT<R>::C *x, const typename CT<R>::C *p, const typename CT<R>::C *q,

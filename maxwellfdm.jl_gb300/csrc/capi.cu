@@ -390,6 +390,10 @@ int fdfd_create(const fdfd_desc *d, fdfd_handle **out) {
   {
     const char *ev = std::getenv("FDFD_DISABLE_TMA");
     h->tma_disabled = ev != nullptr && ev[0] != '\0' && ev[0] != '0';
+    // programmatic dependent launch measured slower on the 96³ solve (the
+    // early-resident dependants take SM slots); opt in with FDFD_PDL=1
+    const char *pd = std::getenv("FDFD_PDL");
+    h->pdl = pd != nullptr && pd[0] != '\0' && pd[0] != '0';
     const char *kc = std::getenv("FDFD_KCHUNK");
     if (kc != nullptr) h->kc_force = std::max(1, std::min(std::atoi(kc), h->N[2]));
   }

@@ -126,6 +126,7 @@ struct fdfd_handle {
   fdfd::KScalars *util_sc = nullptr;  // finalisation target of one-off reductions
   int *dev_err = nullptr;             // set by a kernel whose bounded wait gave up
   bool tma_disabled = false;          // FDFD_DISABLE_TMA=1: plain-load operator kernel only
+  bool pdl = false;                   // programmatic dependent launch (FDFD_PDL=1 enables)
   int kc[2] = {0, 0};                 // tuned z-chunk length: [complex128, complex64]
   int kc_force = 0;                   // FDFD_KCHUNK: fixed z-chunk length (no tuning)
   std::string err;

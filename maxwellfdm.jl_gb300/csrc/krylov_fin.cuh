@@ -167,4 +167,45 @@ template <> struct Acc<float> {
   __device__ __forceinline__ double get() const { return (double)s + (double)c; }
 };
 
+// Short per-thread sum (the operator kernel's epilogue adds at most
+// 3 × z-chunk terms per thread): plain FP32, widened before the FP64
+// block and grid sums.
+template <typename R> struct ShortAcc;
+template <> struct ShortAcc<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double v) { s += v; }
+  __device__ __forceinline__ double get() const { return s; }
+};
+template <> struct ShortAcc<float> {
+  float s = 0.f;
+  __device__ __forceinline__ void add(float v) { s += v; }
+  __device__ __forceinline__ double get() const { return (double)s; }
+};
+
+// Programmatic dependent launch: a kernel lets the next one in the stream
+// start its prologue early (launch_dependents) and waits for the previous
+// kernel's results to be complete and visible (wait) before reading them.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// Launch with programmatic stream serialisation (when h->pdl): the kernel
+// may begin while its predecessor in the stream is finishing; the kernel's
+// own pdl_wait() orders its reads.  Recorded as programmatic edges when the
+// stream is being captured into a CUDA graph.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_k(const fdfd_handle *h, void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                            Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = h->stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = h->pdl ? at : nullptr;
+  cfg.numAttrs = h->pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 }  // namespace fdfd

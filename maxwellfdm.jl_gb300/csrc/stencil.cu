@@ -26,6 +26,10 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+
 #include "krylov_fin.cuh"
 
 namespace fdfd {
@@ -220,7 +224,7 @@ __device__ __forceinline__ R ld_eoff(const OpArgs<R> &a, int p, int gi, int gj, 
 }
 
 template <typename R> struct Accs {
-  Acc<R> r0, i0, r1;
+  ShortAcc<R> r0, i0, r1;
 };
 
 // Operands of the output stage that come from global memory, loaded at the
@@ -372,7 +376,7 @@ __global__ void __launch_bounds__(NTHR) k_apply(OpArgs<R> a, Extra<R> ex, const 
                                                 KScalars *sc) {
   extern __shared__ __align__(16) unsigned char smraw[];
   PlainSmem<R> &S = *reinterpret_cast<PlainSmem<R> *>(smraw);
-  if (sc != nullptr && sc->done) return;
+  pdl_trigger();
 
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
   const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
@@ -383,8 +387,11 @@ __global__ void __launch_bounds__(NTHR) k_apply(OpArgs<R> a, Extra<R> ex, const 
   const long long tilecol = blockIdx.x + (long long)gridDim.x * blockIdx.y;
   Accs<R> acc;
 
-  // preamble: coefficient tables; E(k0−1), E(k0), E(k0+1); H(k0−1)
+  // preamble: coefficient tables (static data, before the dependency wait);
+  // E(k0−1), E(k0), E(k0+1); H(k0−1)
   fill_coef<R>(S.T, a, i0, j0, tid);
+  pdl_wait();
+  if (sc != nullptr && sc->done) return;
   load_plane<R, TRANSPOSE>(S.E, a, ex, x, i0, j0, k0 - 1, (k0 + 2) % 3, tid);
   load_plane<R, TRANSPOSE>(S.E, a, ex, x, i0, j0, k0, k0 % 3, tid);
   load_plane<R, TRANSPOSE>(S.E, a, ex, x, i0, j0, k0 + 1, (k0 + 1) % 3, tid);
@@ -485,7 +492,7 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2) k_apply_tma(cons
   HTile<R> &H = *reinterpret_cast<HTile<R> *>(smraw + G::H_OFF);
   CoefTile<R> &T = *reinterpret_cast<CoefTile<R> *>(smraw + G::T_OFF);
   uint64_t *bars = reinterpret_cast<uint64_t *>(smraw + G::BAR_OFF);
-  if (sc != nullptr && sc->done) return;
+  pdl_trigger();
 
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
   const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
@@ -499,10 +506,15 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2) k_apply_tma(cons
   Accs<R> acc;
   bool ok = true;
 
+  // prologue on static data, overlapping the previous kernel's tail
   if (tid == 0) {
     for (int s = 0; s < G::NSLOT; ++s) mbar_init(smem_u32(&bars[s]), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmap)) : "memory");
   }
+  fill_coef<R>(T, a, i0, j0, tid);
+  pdl_wait();
+  if (sc != nullptr && sc->done) return;
   __syncthreads();
   if (tid == 0) {
     for (int p = 0; p < G::NSLOT; ++p) {
@@ -511,12 +523,22 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2) k_apply_tma(cons
         tma_load_plane(smem_u32(smraw + p * G::SLOT_BYTES), &tmap, cx, cy, q, smem_u32(&bars[p]), G::PLANE_BYTES);
     }
   }
-  fill_coef<R>(T, a, i0, j0, tid);
-  ok = mbar_wait(smem_u32(&bars[0]), 0) && ok;
-  ok = mbar_wait(smem_u32(&bars[1]), 0) && ok;
-  pin_fixup<R>(E, 0, i0, j0, kfirst, tid);
-  pin_fixup<R>(E, 1, i0, j0, k0, tid);
+  // Only warp 0 polls the mbarriers; the block then joins at bar.sync, which
+  // orders the landed tile for every thread (polling from all warps would
+  // burn issue slots the computing warps need).  Pinned-DOF fix-ups run only
+  // in CTAs that touch the low walls.
+  const bool warp0 = tid < 32;
+  const bool wall = (i0 == 0) || (j0 == 0);
+  if (warp0) {
+    ok = mbar_wait(smem_u32(&bars[0]), 0) && ok;
+    ok = mbar_wait(smem_u32(&bars[1]), 0) && ok;
+  }
   __syncthreads();
+  if (wall || k0 == 0) {
+    pin_fixup<R>(E, 0, i0, j0, kfirst, tid);
+    pin_fixup<R>(E, 1, i0, j0, k0, tid);
+    __syncthreads();
+  }
   compute_h<R>(E, H, T, a, kfirst, 0, 1, (k0 + 1) & 1, tid);
 
   for (int k = k0; k < k1; ++k) {
@@ -525,8 +547,11 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2) k_apply_tma(cons
     const int hc = k & 1, hp = (k + 1) & 1;
     Pre<R> pf;
     if (active) prefetch<R, EPI>(pf, a, aux0, gi + (long long)a.N[0] * (gj + (long long)a.N[1] * k));
-    ok = mbar_wait(smem_u32(&bars[s1]), (p1 / G::NSLOT) & 1) && ok;
-    pin_fixup<R>(E, s1, i0, j0, k + 1, tid);
+    if (warp0) ok = mbar_wait(smem_u32(&bars[s1]), (p1 / G::NSLOT) & 1) && ok;
+    if (wall) {
+      __syncthreads();
+      pin_fixup<R>(E, s1, i0, j0, k + 1, tid);
+    }
     __syncthreads();  // E(k+1) present and fixed up, H(k−1) complete
     compute_h<R>(E, H, T, a, k, s0, s1, hc, tid);
     __syncthreads();
@@ -544,10 +569,12 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2) k_apply_tma(cons
     }
   }
   if (!ok) {
-    // a bounded wait gave up: report it and drain this block's copies (bounded)
+    // a bounded wait gave up (warp 0 only): report it and drain this
+    // block's copies, again with bounded waits
     if (tid == 0) atomicExch(errflag, 1);
     for (int s = 0; s < G::NSLOT; ++s) mbar_wait(smem_u32(&bars[s]), 0), mbar_wait(smem_u32(&bars[s]), 1);
   }
+  __syncthreads();  // no thread leaves while warp 0 may still drain copies into this block's memory
   if (EPI != EPI_STORE) {
     block_reduce_finalise<NTHR>(make_double2(acc.r0.get(), acc.i0.get()), make_double2(acc.r1.get(), 0.0), red, fin,
                                 sc);
@@ -703,9 +730,10 @@ static int launch_t(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R>::
     CUtensorMap map;
     int rc = make_map<R>(h, x, &map);
     if (rc) return rc;
-    k_apply_tma<R, EPI><<<grid, block, smem, h->stream>>>(map, a, ex, x, y, aux0, h->red, fin, sc, h->dev_err);
+    const cudaError_t e =
+        launch_k(h, k_apply_tma<R, EPI>, grid, block, (size_t)smem, map, a, ex, x, y, aux0, h->red, fin, sc, h->dev_err);
     h->launches++;
-    return cuda_check(h, cudaGetLastError(), "k_apply_tma launch");
+    return cuda_check(h, e, "k_apply_tma launch");
   }
   static bool attr_set[8] = {false};  // per device ordinal (≤ 8 devices per process)
   const size_t smem = sizeof(PlainSmem<R>);
@@ -714,9 +742,9 @@ static int launch_t(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R>::
     if (e != cudaSuccess) return cuda_check(h, e, "cudaFuncSetAttribute(k_apply)");
     attr_set[d] = true;
   }
-  k_apply<R, EPI, TR><<<grid, block, smem, h->stream>>>(a, ex, x, y, aux0, h->red, fin, sc);
+  const cudaError_t e = launch_k(h, k_apply<R, EPI, TR>, grid, block, smem, a, ex, x, y, aux0, h->red, fin, sc);
   h->launches++;
-  return cuda_check(h, cudaGetLastError(), "k_apply launch");
+  return cuda_check(h, e, "k_apply launch");
 }
 
 // Autotuner for the z-chunk length: times y = A x for each candidate with
@@ -756,21 +784,23 @@ int autotune_kchunk(fdfd_handle *h) {
                                                     FIN_NONE, nullptr, false);
       };
       if ((rc = launch())) break;
-      float total = 0.f;
-      for (int r = 0; r < 3 && rc == FDFD_OK; ++r) {
+      float ts[5];
+      for (int r = 0; r < 5 && rc == FDFD_OK; ++r) {
         cudaMemsetAsync(fl, r, flush_bytes, h->stream);
         cudaEventRecord(h->ev0, h->stream);
         rc = launch();
         cudaEventRecord(h->ev1, h->stream);
         if (rc || (rc = cuda_check(h, cudaEventSynchronize(h->ev1), "autotune sync"))) break;
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, h->ev0, h->ev1);
-        total += ms;
+        cudaEventElapsedTime(&ts[r], h->ev0, h->ev1);
       }
       if (rc) break;
-      if (verbose) fprintf(stderr, "fdfd autotune: %s kchunk %d: %.1f us\n", prec ? "c64" : "c128", kc, total / 3 * 1e3);
-      if (total < best) {
-        best = total;
+      std::sort(ts, ts + 5);
+      const float med = ts[2];
+      if (verbose) fprintf(stderr, "fdfd autotune: %s kchunk %d: %.1f us\n", prec ? "c64" : "c128", kc, med * 1e3);
+      // candidates come in increasing kc (fewer CTAs): take a later one only
+      // if it is clearly faster
+      if (med < 0.97f * best) {
+        best = med;
         best_kc = kc;
       }
     }
