@@ -189,7 +189,16 @@ int finish_eps(fdfd_handle *h) {
     rc = build_oflags(h);
     if (rc) return rc;
   }
-  return cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
+  rc = cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
+  if (rc == FDFD_OK && h->tuned_off >= 0 && h->tuned_off != (h->has_off ? 1 : 0)) {
+    // retune the z-chunk for the new operator; captured graphs hold the old
+    // launch shapes and possibly a reduction buffer that is about to grow
+    drop_graphs(h);
+    if ((rc = autotune_kchunk(h))) return rc;
+    if ((rc = ensure_red(h, apply_blocks(h)))) return rc;
+    rc = cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
+  }
+  return rc;
 }
 
 // eps_diag_aos[c + 3 cell], eps_off_aos[p + 3 cell] (or null) → SoA on device

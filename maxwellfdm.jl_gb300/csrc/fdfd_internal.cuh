@@ -129,6 +129,7 @@ struct fdfd_handle {
   bool pdl = false;                   // programmatic dependent launch (FDFD_PDL=1 enables)
   int kc[2] = {0, 0};                 // tuned z-chunk length: [complex128, complex64]
   int kc_force = 0;                   // FDFD_KCHUNK: fixed z-chunk length (no tuning)
+  int tuned_off = -1;                 // has_off at the last tuning (−1: not tuned yet)
   std::string err;
 };
 
@@ -157,6 +158,8 @@ int autotune_kchunk(fdfd_handle *h);
 int ensure_red(fdfd_handle *h, int blocks);
 
 void free_workspace(fdfd_handle *h);
+// destroy the captured solver graphs (launch shapes or buffers changed)
+void drop_graphs(fdfd_handle *h);
 int smooth_objects_impl(fdfd_handle *h, const double *const lprim[3], const fdfd_object *objs, int nobj,
                         double eps_bg, const fdfd_design *design);
 int upload_eps(fdfd_handle *h, const double *eps_diag_aos, const double *eps_off_aos);

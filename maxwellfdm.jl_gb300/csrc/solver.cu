@@ -95,6 +95,18 @@ void free_workspace(fdfd_handle *h) {
   h->ws = nullptr;
 }
 
+void drop_graphs(fdfd_handle *h) {
+  Workspace *ws = h->ws;
+  if (!ws) return;
+  for (auto &a : ws->gexec)
+    for (auto &b : a)
+      for (auto &g : b)
+        if (g) {
+          cudaGraphExecDestroy(g);
+          g = nullptr;
+        }
+}
+
 static int alloc(fdfd_handle *h, void **p, size_t bytes, const char *what) {
   if (*p) return FDFD_OK;
   cudaError_t e = cudaMalloc(p, bytes);

@@ -54,6 +54,20 @@ struct CoefTile {
   C cmy[TY + 2], cey[TY + 2], wmy[TY + 2], wpy[TY + 2];
 };
 
+// Corner terms of the off-diagonal ε operator for one tile-plane, each
+// computed once and shared by the two outputs that average it:
+//   xc(ii,jj) = ε_xy·⟨E_y⟩ + ε_zx·⟨E_z⟩ at corner (i0+ii, j0+jj, k), ii ∈ [0,T]
+//   yc(ii,jj) = ε_xy·⟨E_x⟩ + ε_yz·⟨E_z⟩ at corner (i0+ii, j0+jj, k), jj ∈ [0,T]
+//   zc[s](ii,jj) = ε_zx·⟨E_x⟩ + ε_yz·⟨E_y⟩ at corner (i0+ii, j0+jj, k'), s = k'&1
+// with ⟨E_v⟩ the s∆l-weighted average of E_v onto the corner.
+template <typename R>
+struct OffTile {
+  using C = typename CT<R>::C;
+  C xc[TY][TX + 1];
+  C yc[TY + 1][TX];
+  C zc[2][TY][TX];
+};
+
 // ---- plain-load ring: SoA by component, 3 slots
 template <typename R>
 struct PlainE {
@@ -66,6 +80,7 @@ struct PlainSmem {
   PlainE<R> E;
   HTile<R> H;
   CoefTile<R> T;
+  OffTile<R> O;
 };
 
 // ---- TMA ring: the global AoS cell layout, 4 slots.  The box starts XOFF
@@ -79,8 +94,21 @@ struct TmaGeom {
   static constexpr int SLOT_BYTES = (PLANE_BYTES + 127) / 128 * 128;
   static constexpr int H_OFF = NSLOT * SLOT_BYTES;
   static constexpr int T_OFF = H_OFF + (int)((sizeof(HTile<R>) + 15) / 16 * 16);
-  static constexpr int BAR_OFF = T_OFF + (int)((sizeof(CoefTile<R>) + 15) / 16 * 16);
+  static constexpr int O_OFF = T_OFF + (int)((sizeof(CoefTile<R>) + 15) / 16 * 16);
+  // complex64 only: a ring slot per plane for the off-diagonal ε of corners
+  // i0 … i0+EOX−1, j0 … j0+TY, laid out [p][jj][ii] (EOX·4 bytes a multiple
+  // of 16); complex128 reads them from global memory (shared memory would
+  // drop it to one CTA per SM)
+  static constexpr int EOX = TX + 4;
+  static constexpr int EO_BYTES = sizeof(R) == 4 ? EOX * (TY + 1) * 3 * (int)sizeof(R) : 0;
+  static constexpr int EO_SLOT = (EO_BYTES + 127) / 128 * 128;
+  // TMA destinations (E slots, ε slots) start on 128-byte boundaries
+  static constexpr int EO_OFF = (O_OFF + (int)sizeof(OffTile<R>) + 127) / 128 * 128;
+  static constexpr int BAR_OFF = EO_OFF + NSLOT * EO_SLOT;
   static constexpr int SMEM = BAR_OFF + NSLOT * 8 + 128;  // + alignment slack
+  static_assert(SLOT_BYTES % 128 == 0 && EO_OFF % 128 == 0 && EO_SLOT % 128 == 0, "TMA destination alignment");
+  static_assert(BAR_OFF % 8 == 0, "mbarrier alignment");
+  static_assert(SMEM <= 227 * 1024, "shared memory per CTA");
 };
 template <typename R>
 struct TmaE {
@@ -100,6 +128,7 @@ struct Extra {
   const C *sdlm[3];   // s∆lₘ per axis
   C ph[3], phinv[3];  // Bloch e^{-ikL} and its inverse
   int kchunk;
+  int eoff_tma;       // TMA kernel: off-diagonal ε staged through the shared-memory ring
 };
 
 template <typename R>
@@ -223,6 +252,83 @@ __device__ __forceinline__ R ld_eoff(const OpArgs<R> &a, int p, int gi, int gj, 
   return a.eoff[(long long)p * a.ncell + gi + (long long)a.N[0] * (gj + (long long)a.N[1] * gk)];
 }
 
+// Off-diagonal ε of one tile-plane: a TMA-staged shared copy [p][jj][ii]
+// (corner (i0+ii, j0+jj); zero beyond the grid, as PEC ghosts are), or —
+// s == nullptr — global memory with the ghost rules of ld_eoff.
+template <typename R>
+struct EoffSrc {
+  const R *s;
+  __device__ __forceinline__ R get(const OpArgs<R> &a, int p, int i0, int j0, int ii, int jj, int k) const {
+    if (s != nullptr) return s[(p * (TY + 1) + jj) * TmaGeom<R>::EOX + ii];
+    return ld_eoff(a, p, i0 + ii, j0 + jj, k);
+  }
+};
+
+// x- and y-directed corner terms of plane k (E(k−1), E(k) in slots sm, s0).
+// A thread owns xc/yc positions tid and tid + NTHR; all its ε loads are
+// issued before any is used, so their latencies overlap.
+template <typename R, typename ET>
+__device__ __forceinline__ void stage_xy(const ET &E, OffTile<R> &O, const CoefTile<R> &T, const OpArgs<R> &a,
+                                         const EoffSrc<R> &src, int i0, int j0, int k, int sm, int s0, int tid) {
+  using C = typename CT<R>::C;
+  constexpr int NXC = TY * (TX + 1), NYC = (TY + 1) * TX;
+  R vx[2][2], vy[2][2];
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const int p = tid + r * NTHR;
+    vx[r][0] = vx[r][1] = vy[r][0] = vy[r][1] = R(0);
+    {
+      // corners no active output reads (beyond the one-past corner) stay 0
+      const int ii = p % (TX + 1), jj = p / (TX + 1);
+      if (p < NXC && i0 + ii <= a.N[0] && j0 + jj < a.N[1]) {
+        vx[r][0] = src.get(a, 0, i0, j0, ii, jj, k);
+        vx[r][1] = src.get(a, 2, i0, j0, ii, jj, k);
+      }
+    }
+    {
+      const int ii = p % TX, jj = p / TX;
+      if (p < NYC && i0 + ii < a.N[0] && j0 + jj <= a.N[1]) {
+        vy[r][0] = src.get(a, 0, i0, j0, ii, jj, k);
+        vy[r][1] = src.get(a, 1, i0, j0, ii, jj, k);
+      }
+    }
+  }
+  const C wmz = a.wm[2][k], wpz = a.wp[2][k];
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const int p = tid + r * NTHR;
+    if (p < NXC) {
+      const int ii = p % (TX + 1), jj = p / (TX + 1);
+      const C ay = cadd(cmul(T.wmy[jj + 1], E.get(s0, 1, jj - 1, ii)), cmul(T.wpy[jj + 1], E.get(s0, 1, jj, ii)));
+      const C az = cadd(cmul(wmz, E.get(sm, 2, jj, ii)), cmul(wpz, E.get(s0, 2, jj, ii)));
+      O.xc[jj][ii] = cadd(cscale(ay, vx[r][0]), cscale(az, vx[r][1]));
+    }
+    if (p < NYC) {
+      const int ii = p % TX, jj = p / TX;
+      const C ax = cadd(cmul(T.wmx[ii + 1], E.get(s0, 0, jj, ii - 1)), cmul(T.wpx[ii + 1], E.get(s0, 0, jj, ii)));
+      const C az = cadd(cmul(wmz, E.get(sm, 2, jj, ii)), cmul(wpz, E.get(s0, 2, jj, ii)));
+      O.yc[jj][ii] = cadd(cscale(ax, vy[r][0]), cscale(az, vy[r][1]));
+    }
+  }
+}
+
+// z-directed corner terms of plane kz (E(kz) in slot sz) into zc[kz & 1];
+// one position per thread (NTHR = TX·TY).
+template <typename R, typename ET>
+__device__ __forceinline__ void stage_z(const ET &E, OffTile<R> &O, const CoefTile<R> &T, const OpArgs<R> &a,
+                                        const EoffSrc<R> &src, int i0, int j0, int kz, int sz, int tid) {
+  using C = typename CT<R>::C;
+  const int ii = tid % TX, jj = tid / TX;
+  R v0 = R(0), v1 = R(0);
+  if (i0 + ii < a.N[0] && j0 + jj < a.N[1]) {
+    v0 = src.get(a, 2, i0, j0, ii, jj, kz);
+    v1 = src.get(a, 1, i0, j0, ii, jj, kz);
+  }
+  const C ax = cadd(cmul(T.wmx[ii + 1], E.get(sz, 0, jj, ii - 1)), cmul(T.wpx[ii + 1], E.get(sz, 0, jj, ii)));
+  const C ay = cadd(cmul(T.wmy[jj + 1], E.get(sz, 1, jj - 1, ii)), cmul(T.wpy[jj + 1], E.get(sz, 1, jj, ii)));
+  O.zc[kz & 1][jj][ii] = cadd(cscale(ax, v0), cscale(ay, v1));
+}
+
 template <typename R> struct Accs {
   ShortAcc<R> r0, i0, r1;
 };
@@ -252,8 +358,9 @@ __device__ __forceinline__ void prefetch(Pre<R> &pf, const OpArgs<R> &a, const t
 
 // y(k) at the thread's cell (gi, gj, k) from shared memory.
 template <typename R, int EPI, bool TRANSPOSE, typename ET>
-__device__ __forceinline__ void output_cell(const ET &E, const HTile<R> &H, const CoefTile<R> &T, const OpArgs<R> &a,
-                                            const Extra<R> &ex, const Pre<R> &pf,
+__device__ __forceinline__ void output_cell(const ET &E, const HTile<R> &H, const CoefTile<R> &T,
+                                            const OffTile<R> &O, const OpArgs<R> &a, const Extra<R> &ex,
+                                            const Pre<R> &pf,
                                             const typename CT<R>::C *__restrict__ x,
                                             typename CT<R>::C *__restrict__ y, int gi, int gj, int k, int tx, int ty,
                                             int sm, int s0, int s1, int hc, int hp, bool offd, Accs<R> &acc) {
@@ -284,37 +391,10 @@ __device__ __forceinline__ void output_cell(const ET &E, const HTile<R> &H, cons
   C dy = cscale(e_y, pf.e1);
   C dz = cscale(e_z, pf.e2);
   if (offd) {
-    const C wmz = a.wm[2][k], wpz = a.wp[2][k];
-    const C wmx = T.wmx[tx + 1], wpx = T.wpx[tx + 1], wmy = T.wmy[ty + 1], wpy = T.wpy[ty + 1];
-    C ox = czero<C>(), oy = czero<C>(), oz = czero<C>();
-    // x output: corners (i', j, k), i' ∈ {i, i+1}
-#pragma unroll
-    for (int s = 0; s < 2; ++s) {
-      const C eym = E.get(s0, 1, ty - 1, tx + s), eyp = E.get(s0, 1, ty, tx + s);
-      const C ezm = E.get(sm, 2, ty, tx + s), ezp = E.get(s0, 2, ty, tx + s);
-      const R exy = ld_eoff(a, 0, gi + s, gj, k), ezx = ld_eoff(a, 2, gi + s, gj, k);
-      ox = cadd(ox, cscale(cadd(cmul(wmy, eym), cmul(wpy, eyp)), exy));
-      ox = cadd(ox, cscale(cadd(cmul(wmz, ezm), cmul(wpz, ezp)), ezx));
-    }
-    // y output: corners (i, j', k), j' ∈ {j, j+1}
-#pragma unroll
-    for (int s = 0; s < 2; ++s) {
-      const C exm = E.get(s0, 0, ty + s, tx - 1), exp_ = E.get(s0, 0, ty + s, tx);
-      const C ezm = E.get(sm, 2, ty + s, tx), ezp = E.get(s0, 2, ty + s, tx);
-      const R exy = ld_eoff(a, 0, gi, gj + s, k), eyz = ld_eoff(a, 1, gi, gj + s, k);
-      oy = cadd(oy, cscale(cadd(cmul(wmx, exm), cmul(wpx, exp_)), exy));
-      oy = cadd(oy, cscale(cadd(cmul(wmz, ezm), cmul(wpz, ezp)), eyz));
-    }
-    // z output: corners (i, j, k'), k' ∈ {k, k+1}
-#pragma unroll
-    for (int s = 0; s < 2; ++s) {
-      const int sl = s ? s1 : s0;
-      const C exm = E.get(sl, 0, ty, tx - 1), exp_ = E.get(sl, 0, ty, tx);
-      const C eym = E.get(sl, 1, ty - 1, tx), eyp = E.get(sl, 1, ty, tx);
-      const R ezx = ld_eoff(a, 2, gi, gj, k + s), eyz = ld_eoff(a, 1, gi, gj, k + s);
-      oz = cadd(oz, cscale(cadd(cmul(wmx, exm), cmul(wpx, exp_)), ezx));
-      oz = cadd(oz, cscale(cadd(cmul(wmy, eym), cmul(wpy, eyp)), eyz));
-    }
+    // each output averages the two staged corner terms around it (weight ½)
+    const C ox = cadd(O.xc[ty][tx], O.xc[ty][tx + 1]);
+    const C oy = cadd(O.yc[ty][tx], O.yc[ty + 1][tx]);
+    const C oz = cadd(O.zc[k & 1][ty][tx], O.zc[(k + 1) & 1][ty][tx]);
     if (!pinx) dx = cadd(dx, cscale(ox, R(0.5)));
     if (!piny) dy = cadd(dy, cscale(oy, R(0.5)));
     if (!pinz) dz = cadd(dz, cscale(oz, R(0.5)));
@@ -397,6 +477,7 @@ __global__ void __launch_bounds__(NTHR) k_apply(OpArgs<R> a, Extra<R> ex, const 
   load_plane<R, TRANSPOSE>(S.E, a, ex, x, i0, j0, k0 + 1, (k0 + 1) % 3, tid);
   __syncthreads();
   compute_h<R>(S.E, S.H, S.T, a, k0 - 1, (k0 + 2) % 3, k0 % 3, (k0 + 1) & 1, tid);
+  bool zvalid = false;  // zc[k & 1] already holds plane k's z-directed corners
 
   for (int k = k0; k < k1; ++k) {
     const int sm = (k + 2) % 3, s0 = k % 3, s1 = (k + 1) % 3;
@@ -405,10 +486,18 @@ __global__ void __launch_bounds__(NTHR) k_apply(OpArgs<R> a, Extra<R> ex, const 
     if (active) prefetch<R, EPI>(pf, a, aux0, gi + (long long)a.N[0] * (gj + (long long)a.N[1] * k));
     __syncthreads();  // E(k+1) present, H(k−1) complete
     compute_h<R>(S.E, S.H, S.T, a, k, s0, s1, hc, tid);
+    const bool offd = offd_on(a, tilecol, k);
+    if (offd) {
+      const EoffSrc<R> g{nullptr};
+      stage_xy<R>(S.E, S.O, S.T, a, g, i0, j0, k, sm, s0, tid);
+      if (!zvalid) stage_z<R>(S.E, S.O, S.T, a, g, i0, j0, k, s0, tid);
+      stage_z<R>(S.E, S.O, S.T, a, g, i0, j0, k + 1, s1, tid);
+    }
+    zvalid = offd;
     __syncthreads();
     if (active)
-      output_cell<R, EPI, TRANSPOSE>(S.E, S.H, S.T, a, ex, pf, x, y, gi, gj, k, tx, ty, sm, s0, s1, hc, hp,
-                                     offd_on(a, tilecol, k), acc);
+      output_cell<R, EPI, TRANSPOSE>(S.E, S.H, S.T, S.O, a, ex, pf, x, y, gi, gj, k, tx, ty, sm, s0, s1, hc, hp,
+                                     offd, acc);
     __syncthreads();  // everyone done with E(k−1) and H(k−1)
     if (k + 1 < k1) load_plane<R, TRANSPOSE>(S.E, a, ex, x, i0, j0, k + 2, sm, tid);
   }
@@ -424,13 +513,23 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)_
 __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
 }
-__device__ __forceinline__ void tma_load_plane(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2,
-                                               uint32_t bar, uint32_t bytes) {
+__device__ __forceinline__ void mbar_expect(uint32_t bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void tma_copy3d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2,
+                                           uint32_t bar) {
   asm volatile(
       "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
       "[%5];" ::"r"(dst),
       "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void tma_copy4d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
+                                           uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
       : "memory");
 }
 // Bounded wait on an mbarrier phase: gives up after ~2^31 SM clocks (about
@@ -478,9 +577,29 @@ __device__ __forceinline__ void pin_fixup(const TmaE<R> &E, int slot, int i0, in
   }
 }
 
+// Issue the copies of plane q into ring slot `slot` (one thread): the E
+// tile and, when the TMA kernel stages the off-diagonal ε and plane q or
+// q−1 is flagged (the z-directed corners of q serve both), the ε tile too —
+// both completing on the slot's mbarrier.
+template <typename R>
+__device__ __forceinline__ void issue_plane(unsigned char *smraw, uint64_t *bars, const CUtensorMap *tmap,
+                                            const CUtensorMap *emap, const OpArgs<R> &a, const Extra<R> &ex,
+                                            long long tilecol, int cx, int cy, int i0, int j0, int k0, int q,
+                                            int slot) {
+  using G = TmaGeom<R>;
+  bool eo = false;
+  if (G::EO_SLOT > 0 && ex.eoff_tma && q >= k0)
+    eo = (q < a.N[2] && offd_on(a, tilecol, q)) || (q >= 1 && offd_on(a, tilecol, q - 1));
+  const uint32_t bar = smem_u32(&bars[slot]);
+  mbar_expect(bar, (uint32_t)(G::PLANE_BYTES + (eo ? G::EO_BYTES : 0)));
+  tma_copy3d(smem_u32(smraw + slot * G::SLOT_BYTES), tmap, cx, cy, q, bar);
+  if (eo) tma_copy4d(smem_u32(smraw + G::EO_OFF + slot * G::EO_SLOT), emap, i0, j0, q, 0, bar);
+}
+
 template <typename R, int EPI>
-__global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2) k_apply_tma(const __grid_constant__ CUtensorMap tmap, OpArgs<R> a,
-                                                    Extra<R> ex, const typename CT<R>::C *__restrict__ x,
+__global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2)
+    k_apply_tma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap emap, OpArgs<R> a,
+                Extra<R> ex, const typename CT<R>::C *__restrict__ x,
                                                     typename CT<R>::C *__restrict__ y,
                                                     const typename CT<R>::C *__restrict__ aux0, RedBuf red, int fin,
                                                     KScalars *sc, int *errflag) {
@@ -491,6 +610,7 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2) k_apply_tma(cons
   TmaE<R> E{smraw};
   HTile<R> &H = *reinterpret_cast<HTile<R> *>(smraw + G::H_OFF);
   CoefTile<R> &T = *reinterpret_cast<CoefTile<R> *>(smraw + G::T_OFF);
+  OffTile<R> &O = *reinterpret_cast<OffTile<R> *>(smraw + G::O_OFF);
   uint64_t *bars = reinterpret_cast<uint64_t *>(smraw + G::BAR_OFF);
   pdl_trigger();
 
@@ -511,6 +631,7 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2) k_apply_tma(cons
     for (int s = 0; s < G::NSLOT; ++s) mbar_init(smem_u32(&bars[s]), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmap)) : "memory");
+    if (ex.eoff_tma) asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&emap)) : "memory");
   }
   fill_coef<R>(T, a, i0, j0, tid);
   pdl_wait();
@@ -520,7 +641,7 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2) k_apply_tma(cons
     for (int p = 0; p < G::NSLOT; ++p) {
       const int q = kfirst + p;
       if (q <= k1)
-        tma_load_plane(smem_u32(smraw + p * G::SLOT_BYTES), &tmap, cx, cy, q, smem_u32(&bars[p]), G::PLANE_BYTES);
+        issue_plane<R>(smraw, bars, &tmap, &emap, a, ex, tilecol, cx, cy, i0, j0, k0, q, p);
     }
   }
   // Only warp 0 polls the mbarriers; the block then joins at bar.sync, which
@@ -540,6 +661,7 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2) k_apply_tma(cons
     __syncthreads();
   }
   compute_h<R>(E, H, T, a, kfirst, 0, 1, (k0 + 1) & 1, tid);
+  bool zvalid = false;  // zc[k & 1] already holds plane k's z-directed corners
 
   for (int k = k0; k < k1; ++k) {
     const int pm = k - 1 - kfirst, p0 = k - kfirst, p1 = k + 1 - kfirst;
@@ -554,17 +676,25 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2) k_apply_tma(cons
     }
     __syncthreads();  // E(k+1) present and fixed up, H(k−1) complete
     compute_h<R>(E, H, T, a, k, s0, s1, hc, tid);
+    const bool offd = offd_on(a, tilecol, k);
+    if (offd) {
+      const bool eo = G::EO_SLOT > 0 && ex.eoff_tma;
+      const EoffSrc<R> e0{eo ? reinterpret_cast<const R *>(smraw + G::EO_OFF + s0 * G::EO_SLOT) : nullptr};
+      const EoffSrc<R> e1{eo ? reinterpret_cast<const R *>(smraw + G::EO_OFF + s1 * G::EO_SLOT) : nullptr};
+      stage_xy<R>(E, O, T, a, e0, i0, j0, k, sm, s0, tid);
+      if (!zvalid) stage_z<R>(E, O, T, a, e0, i0, j0, k, s0, tid);
+      stage_z<R>(E, O, T, a, e1, i0, j0, k + 1, s1, tid);
+    }
+    zvalid = offd;
     __syncthreads();
     if (active)
-      output_cell<R, EPI, false>(E, H, T, a, ex, pf, x, y, gi, gj, k, tx, ty, sm, s0, s1, hc, hp,
-                                 offd_on(a, tilecol, k), acc);
+      output_cell<R, EPI, false>(E, H, T, O, a, ex, pf, x, y, gi, gj, k, tx, ty, sm, s0, s1, hc, hp, offd, acc);
     __syncthreads();  // slot of E(k−1) is free
     if (tid == 0) {
       const int q = k + 3;
       if (q <= k1) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        tma_load_plane(smem_u32(smraw + sm * G::SLOT_BYTES), &tmap, cx, cy, q, smem_u32(&bars[sm]),
-                       G::PLANE_BYTES);
+        issue_plane<R>(smraw, bars, &tmap, &emap, a, ex, tilecol, cx, cy, i0, j0, k0, q, sm);
       }
     }
   }
@@ -647,6 +777,7 @@ static Extra<R> make_extra(const fdfd_handle *h) {
   using C = typename CT<R>::C;
   Extra<R> ex;
   ex.kchunk = kchunk_for(h, sizeof(R) == 4);
+  ex.eoff_tma = 0;
   const C *coef;
   if constexpr (sizeof(R) == 8) coef = reinterpret_cast<const C *>(h->coef64);
   else coef = reinterpret_cast<const C *>(h->coef32);
@@ -703,10 +834,30 @@ static int make_map(fdfd_handle *h, const void *x, CUtensorMap *map) {
   return FDFD_OK;
 }
 
+// Off-diagonal ε (complex64 operator) as a 4D tensor (x, y, z, pair) for the
+// shared-memory ring; needs an x pitch that is a multiple of 16 bytes.
+static bool emap_ok(const fdfd_handle *h) {
+  return h->has_off && h->eoff32 != nullptr && (h->N[0] % 4) == 0 &&
+         (reinterpret_cast<uintptr_t>(h->eoff32) & 15) == 0;
+}
+static int make_emap(fdfd_handle *h, CUtensorMap *map) {
+  using G = TmaGeom<float>;
+  const cuuint64_t dims[4] = {(cuuint64_t)h->N[0], (cuuint64_t)h->N[1], (cuuint64_t)h->N[2], 3};
+  const cuuint64_t strides[3] = {(cuuint64_t)h->N[0] * 4, (cuuint64_t)h->N[0] * h->N[1] * 4,
+                                 (cuuint64_t)h->ncell * 4};
+  const cuuint32_t box[4] = {(cuuint32_t)G::EOX, (cuuint32_t)(TY + 1), 1u, 3u};
+  const cuuint32_t estr[4] = {1u, 1u, 1u, 1u};
+  CUresult r = encode_fn()(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, h->eoff32, dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_error(h, FDFD_ERR_CUDA, "cuTensorMapEncodeTiled(eps off-diagonal) failed");
+  return FDFD_OK;
+}
+
 template <typename R, int EPI, bool TR>
 static int launch_t(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R>::C *y,
                     const typename CT<R>::C *aux0, int fin, KScalars *sc) {
-  const Extra<R> ex = make_extra<R>(h);
+  Extra<R> ex = make_extra<R>(h);
   dim3 grid((h->N[0] + TX - 1) / TX, (h->N[1] + TY - 1) / TY, (h->N[2] + ex.kchunk - 1) / ex.kchunk);
   dim3 block(TX, TY, 1);
   const OpArgs<R> a = op_args<R>(h);
@@ -727,11 +878,16 @@ static int launch_t(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R>::
       if (e != cudaSuccess) return cuda_check(h, e, "cudaFuncSetAttribute(carveout)");
       attr_tma[d] = true;
     }
-    CUtensorMap map;
+    CUtensorMap map, emap;
     int rc = make_map<R>(h, x, &map);
     if (rc) return rc;
-    const cudaError_t e =
-        launch_k(h, k_apply_tma<R, EPI>, grid, block, (size_t)smem, map, a, ex, x, y, aux0, h->red, fin, sc, h->dev_err);
+    emap = map;  // placeholder unless the ε ring is used
+    if (sizeof(R) == 4 && emap_ok(h)) {
+      if ((rc = make_emap(h, &emap))) return rc;
+      ex.eoff_tma = 1;
+    }
+    const cudaError_t e = launch_k(h, k_apply_tma<R, EPI>, grid, block, (size_t)smem, map, emap, a, ex, x, y, aux0,
+                                   h->red, fin, sc, h->dev_err);
     h->launches++;
     return cuda_check(h, e, "k_apply_tma launch");
   }
@@ -751,8 +907,9 @@ static int launch_t(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R>::
 // CUDA events on the handle's stream — one warm-up, then three launches each
 // preceded by an L2 flush (a 192 MiB memset, larger than the 129 MB L2), so
 // the choice holds for inputs streamed from HBM — and keeps the fastest,
-// separately for complex64 and complex128.  Runs once at fdfd_create, before
-// any solve is captured into a CUDA graph.
+// separately for complex64 and complex128.  Runs at fdfd_create (vacuum ε)
+// and again whenever new ε data switches the off-diagonal tensor on or off,
+// since the corner-term work changes the best chunk length.
 int autotune_kchunk(fdfd_handle *h) {
   if (h->kc_force > 0) return FDFD_OK;
   const size_t n = 3 * (size_t)h->ncell;
@@ -811,6 +968,7 @@ int autotune_kchunk(fdfd_handle *h) {
   cudaFree(fl);
   h->launches = 0;
   if (rc == FDFD_OK) rc = check_dev_err(h);
+  if (rc == FDFD_OK) h->tuned_off = h->has_off ? 1 : 0;
   return rc;
 }
 
