@@ -185,14 +185,44 @@ int fdfd_solve_dev(fdfd_handle *h, const void *b, void *x,
                    const fdfd_solve_opts *opts, fdfd_stats *stats);
 void fdfd_default_opts(fdfd_solve_opts *opts);
 
+/* ---- field post-processing -------------------------------------------------
+ * H = (i/ω)·(Cₑ e + jₘ): h_from_e (model.jl:276-279) with Pμ = I.  jm may be
+ * NULL (jₘ = 0).  e, jm, hout: complex, 2·3·Ncell doubles, H_w at the H_w
+ * sample of each cell.  Host buffers; the _dev form takes double2 device
+ * buffers and runs asynchronously on the handle's stream. */
+int fdfd_h_from_e(fdfd_handle *h, const double *e, const double *jm, double *hout);
+int fdfd_h_from_e_dev(fdfd_handle *h, const void *e, const void *jm, void *hout);
+/* Corner interpolation of create_Mcs (model.jl:287-306): field = FDFD_EE
+ * applies Mcₑ (E_w averaged backward along w onto the primal voxel corner,
+ * weights s∆lₘ / (2 s∆lₑ)); FDFD_HH applies Mcₘ (H_w averaged forward along w
+ * onto the dual corner, weights s∆lₑ / (2 s∆lₘ)).  in, out: complex,
+ * 2·3·Ncell doubles. */
+int fdfd_corner_mean(fdfd_handle *h, int32_t field, const double *in, double *out);
+int fdfd_corner_mean_dev(fdfd_handle *h, int32_t field, const void *in, void *out);
+
 /* ---- adjoint gradient --------------------------------------------------------
- * For A e = b and a real objective L(e) with g = ∂L/∂e (holomorphic
- * derivative, interleaved complex), solves Aᵀ λ = g and returns
- * dL/dε_ww at every E_w sample: grad[c + 3·cell] = 2·ω²·Re(λ_c·e_c) ... as
- * defined in the design notes (sign convention included).  e, g, grad are
- * host buffers. */
+ * No counterpart in the reference, which only assembles A (create_A,
+ * model.jl:238-259) and leaves differentiation to its users.  For A e = b and
+ * a real objective L(e), pass g = ∂L/∂e, the Wirtinger derivative
+ * ½(∂L/∂Re e − i·∂L/∂Im e) (so that dL = 2·Re(gᵀ de)); e.g. for
+ * L = |Fᴴe|², g = conj(Fᴴe)·conj(F).  The call solves Aᵀ λ = g with BiCGSTAB
+ * (opts: tol, precision, maxit; opts->transpose is ignored) and returns
+ *     grad[c + 3·cell] = dL/dε_cc = 2·Re(ω²·λ_c·e_c)
+ * at every E_c sample (∂A/∂ε_cc = −ω²).  e, g: complex (2·3·Ncell doubles);
+ * grad: 3·Ncell doubles.  Host buffers. */
 int fdfd_eps_grad(fdfd_handle *h, const double *e, const double *g, double *grad,
                   const fdfd_solve_opts *opts, fdfd_stats *stats);
+/* Device-buffer form: e, g, lam are double2[3·Ncell] (lam receives λ),
+ * grad double[3·Ncell]; returns after the handle's stream has finished. */
+int fdfd_eps_grad_dev(fdfd_handle *h, const void *e, const void *g, void *lam, double *grad,
+                      const fdfd_solve_opts *opts, fdfd_stats *stats);
+/* Chain dL/dε_ww (grad as returned above) to the cells of the design region
+ * that the last fdfd_smooth_objects call applied: the sample value there is
+ * the mean of the 4 cells around the E_w edge, so dgrad[cell] collects ¼ of
+ * every sample gradient whose mean includes the cell.  dgrad holds
+ * (hi−lo) cells, x fastest.  FDFD_ERR_ARG without a design region. */
+int fdfd_design_grad(fdfd_handle *h, const double *grad, double *dgrad);
+int fdfd_design_grad_dev(fdfd_handle *h, const double *grad, double *dgrad);
 
 #ifdef __cplusplus
 }

@@ -85,6 +85,14 @@ SIGNATURES = {
     "fdfd_residual_dev_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                             C.POINTER(C.c_double)]),
     "fdfd_eps_grad": (C.c_int, [C.c_void_p, _dp, _dp, _dp, C.POINTER(fdfd_solve_opts), C.POINTER(fdfd_stats)]),
+    "fdfd_eps_grad_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.POINTER(fdfd_solve_opts), C.POINTER(fdfd_stats)]),
+    "fdfd_design_grad": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "fdfd_h_from_e": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
+    "fdfd_h_from_e_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fdfd_corner_mean": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp]),
+    "fdfd_corner_mean_dev": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
+    "fdfd_design_grad_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
 }
 
 

@@ -216,6 +216,7 @@ int upload_eps(fdfd_handle *h, const double *eps_diag_aos, const double *eps_off
                   "upload eps");
   if (rc) return rc;
   h->has_off = off;
+  h->has_design = false;  // explicit ε replaces any smoothed design region
   if (off) {
     for (long long cell = 0; cell < nc; ++cell)
       for (int p = 0; p < 3; ++p) soa[p * nc + cell] = eps_off_aos[p + 3 * cell];
@@ -428,6 +429,7 @@ void fdfd_destroy(fdfd_handle *h) {
   cudaFree(h->smask);
   cudaFree(h->vx64);
   cudaFree(h->vy64);
+  cudaFree(h->ve64);
   cudaFree(h->vx32);
   cudaFree(h->vy32);
   cudaFree(h->red.part);
@@ -625,10 +627,131 @@ int fdfd_solve(fdfd_handle *h, const double *b, double *x, int32_t nrhs, const f
   return FDFD_OK;
 }
 
+int fdfd_eps_grad_dev(fdfd_handle *h, const void *e, const void *g, void *lam, double *grad,
+                      const fdfd_solve_opts *opts, fdfd_stats *stats) {
+  if (!h || !e || !g || !lam || !grad) return set_error(h, FDFD_ERR_ARG, "null argument");
+  int rc = check_opts(h, opts);
+  if (rc) return rc;
+  if (opts->method != FDFD_BICGSTAB) return set_error(h, FDFD_ERR_UNSUPPORTED, "the adjoint solve uses BiCGSTAB");
+  if (!transpose_ok(h)) return set_error(h, FDFD_ERR_UNSUPPORTED, "adjoint with a Bloch phase");
+  cudaSetDevice(h->dev);
+  rc = eps_grad_dev_impl(h, (const double2 *)e, (const double2 *)g, (double2 *)lam, grad, opts, stats);
+  if (rc) return rc;
+  return cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
+}
+
 int fdfd_eps_grad(fdfd_handle *h, const double *e, const double *g, double *grad, const fdfd_solve_opts *opts,
                   fdfd_stats *stats) {
-  (void)e; (void)g; (void)grad; (void)opts; (void)stats;
-  return set_error(h, FDFD_ERR_UNSUPPORTED, "fdfd_eps_grad is not available in this build yet");
+  if (!h || !e || !g || !grad) return set_error(h, FDFD_ERR_ARG, "null argument");
+  int rc = check_opts(h, opts);
+  if (rc) return rc;
+  if (opts->method != FDFD_BICGSTAB) return set_error(h, FDFD_ERR_UNSUPPORTED, "the adjoint solve uses BiCGSTAB");
+  if (!transpose_ok(h)) return set_error(h, FDFD_ERR_UNSUPPORTED, "adjoint with a Bloch phase");
+  cudaSetDevice(h->dev);
+  if ((rc = ensure_scratch(h, false))) return rc;
+  const long long n = 3 * h->ncell;
+  if (!h->ve64 && cudaMalloc(&h->ve64, n * sizeof(double2)) != cudaSuccess) {
+    cudaGetLastError();
+    h->ve64 = nullptr;
+    return set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(adjoint scratch) failed");
+  }
+  if ((rc = cuda_check(h, cudaMemcpyAsync(h->ve64, e, n * sizeof(double2), cudaMemcpyHostToDevice, h->stream),
+                       "H2D e")))
+    return rc;
+  if ((rc = cuda_check(h, cudaMemcpyAsync(h->vx64, g, n * sizeof(double2), cudaMemcpyHostToDevice, h->stream),
+                       "H2D g")))
+    return rc;
+  // λ → vy64; the gradient overwrites g's buffer (g is consumed by the solve)
+  double *dgrad = reinterpret_cast<double *>(h->vx64);
+  rc = eps_grad_dev_impl(h, h->ve64, h->vx64, h->vy64, dgrad, opts, stats);
+  if (rc) return rc;
+  if ((rc = cuda_check(h, cudaMemcpyAsync(grad, dgrad, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream),
+                       "D2H grad")))
+    return rc;
+  return cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
+}
+
+static int ensure_ve(fdfd_handle *h) {
+  if (h->ve64) return FDFD_OK;
+  if (cudaMalloc(&h->ve64, 3 * (size_t)h->ncell * sizeof(double2)) != cudaSuccess) {
+    cudaGetLastError();
+    h->ve64 = nullptr;
+    return set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(field scratch) failed");
+  }
+  return FDFD_OK;
+}
+
+int fdfd_h_from_e_dev(fdfd_handle *h, const void *e, const void *jm, void *hout) {
+  if (!h || !e || !hout) return set_error(h, FDFD_ERR_ARG, "null argument");
+  cudaSetDevice(h->dev);
+  return h_from_e_dev_impl(h, (const double2 *)e, (const double2 *)jm, (double2 *)hout);
+}
+
+int fdfd_h_from_e(fdfd_handle *h, const double *e, const double *jm, double *hout) {
+  if (!h || !e || !hout) return set_error(h, FDFD_ERR_ARG, "null argument");
+  cudaSetDevice(h->dev);
+  int rc = ensure_scratch(h, false);
+  if (!rc && jm) rc = ensure_ve(h);
+  if (rc) return rc;
+  const size_t bytes = 3 * (size_t)h->ncell * sizeof(double2);
+  if ((rc = cuda_check(h, cudaMemcpyAsync(h->vx64, e, bytes, cudaMemcpyHostToDevice, h->stream), "H2D e"))) return rc;
+  if (jm && (rc = cuda_check(h, cudaMemcpyAsync(h->ve64, jm, bytes, cudaMemcpyHostToDevice, h->stream), "H2D jm")))
+    return rc;
+  if ((rc = h_from_e_dev_impl(h, h->vx64, jm ? h->ve64 : nullptr, h->vy64))) return rc;
+  if ((rc = cuda_check(h, cudaMemcpyAsync(hout, h->vy64, bytes, cudaMemcpyDeviceToHost, h->stream), "D2H h")))
+    return rc;
+  return cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
+}
+
+int fdfd_corner_mean_dev(fdfd_handle *h, int32_t field, const void *in, void *out) {
+  if (!h || !in || !out) return set_error(h, FDFD_ERR_ARG, "null argument");
+  if (field != FDFD_EE && field != FDFD_HH) return set_error(h, FDFD_ERR_ARG, "field must be FDFD_EE or FDFD_HH");
+  cudaSetDevice(h->dev);
+  return corner_mean_dev_impl(h, field == FDFD_HH, (const double2 *)in, (double2 *)out);
+}
+
+int fdfd_corner_mean(fdfd_handle *h, int32_t field, const double *in, double *out) {
+  if (!h || !in || !out) return set_error(h, FDFD_ERR_ARG, "null argument");
+  if (field != FDFD_EE && field != FDFD_HH) return set_error(h, FDFD_ERR_ARG, "field must be FDFD_EE or FDFD_HH");
+  cudaSetDevice(h->dev);
+  int rc = ensure_scratch(h, false);
+  if (rc) return rc;
+  const size_t bytes = 3 * (size_t)h->ncell * sizeof(double2);
+  if ((rc = cuda_check(h, cudaMemcpyAsync(h->vx64, in, bytes, cudaMemcpyHostToDevice, h->stream), "H2D field")))
+    return rc;
+  if ((rc = corner_mean_dev_impl(h, field == FDFD_HH, h->vx64, h->vy64))) return rc;
+  if ((rc = cuda_check(h, cudaMemcpyAsync(out, h->vy64, bytes, cudaMemcpyDeviceToHost, h->stream), "D2H corners")))
+    return rc;
+  return cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
+}
+
+int fdfd_design_grad_dev(fdfd_handle *h, const double *grad, double *dgrad) {
+  if (!h || !grad || !dgrad) return set_error(h, FDFD_ERR_ARG, "null argument");
+  cudaSetDevice(h->dev);
+  int rc = design_grad_dev_impl(h, grad, dgrad);
+  if (rc) return rc;
+  return cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
+}
+
+int fdfd_design_grad(fdfd_handle *h, const double *grad, double *dgrad) {
+  if (!h || !grad || !dgrad) return set_error(h, FDFD_ERR_ARG, "null argument");
+  if (!h->has_design) return set_error(h, FDFD_ERR_ARG, "no design region (set one with fdfd_smooth_objects)");
+  cudaSetDevice(h->dev);
+  int rc = ensure_scratch(h, false);
+  if (rc) return rc;
+  const long long n = 3 * h->ncell;
+  long long ne = 1;
+  for (int a = 0; a < 3; ++a) ne *= h->design_hi[a] - h->design_lo[a];
+  double *dg = reinterpret_cast<double *>(h->vx64);
+  double *dout = reinterpret_cast<double *>(h->vy64);
+  if ((rc = cuda_check(h, cudaMemcpyAsync(dg, grad, n * sizeof(double), cudaMemcpyHostToDevice, h->stream),
+                       "H2D grad")))
+    return rc;
+  if ((rc = design_grad_dev_impl(h, dg, dout))) return rc;
+  if ((rc = cuda_check(h, cudaMemcpyAsync(dgrad, dout, ne * sizeof(double), cudaMemcpyDeviceToHost, h->stream),
+                       "D2H design grad")))
+    return rc;
+  return cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
 }
 
 }  // extern "C"

@@ -115,8 +115,11 @@ struct fdfd_handle {
   uint8_t *oflag = nullptr;
   bool has_off = false;
   uint8_t *smask = nullptr;  // 4*ncell smoothing mask (from fdfd_smooth_objects)
+  bool has_design = false;   // a design region was applied by fdfd_smooth_objects
+  int design_lo[3] = {0, 0, 0}, design_hi[3] = {0, 0, 0};
   // scratch for host-pointer entry points
   double2 *vx64 = nullptr, *vy64 = nullptr;
+  double2 *ve64 = nullptr;  // adjoint entry point: the forward field
   float2 *vx32 = nullptr, *vy32 = nullptr;
   fdfd::RedBuf red{nullptr, nullptr};
   int red_blocks = 0;
@@ -163,6 +166,13 @@ void drop_graphs(fdfd_handle *h);
 int smooth_objects_impl(fdfd_handle *h, const double *const lprim[3], const fdfd_object *objs, int nobj,
                         double eps_bg, const fdfd_design *design);
 int upload_eps(fdfd_handle *h, const double *eps_diag_aos, const double *eps_off_aos);
+// adjoint.cu
+int eps_grad_dev_impl(fdfd_handle *h, const double2 *e, const double2 *g, double2 *lam, double *grad,
+                      const fdfd_solve_opts *opts, fdfd_stats *stats);
+int design_grad_dev_impl(fdfd_handle *h, const double *grad, double *out);
+// fields.cu
+int h_from_e_dev_impl(fdfd_handle *h, const double2 *e, const double2 *jm, double2 *hout);
+int corner_mean_dev_impl(fdfd_handle *h, int hfield, const double2 *in, double2 *out);
 int build_oflags(fdfd_handle *h);
 
 }  // namespace fdfd

@@ -1,0 +1,115 @@
+// Field post-processing on the device:
+//   * h_from_e — H = (i/ω)·Pμ⁻¹·(Cₑ e + jₘ)        (src/model/model.jl:276-279,
+//     Pμ = I): the forward-difference curl E→H of the operator, one pass;
+//   * corner means — the create_Mcs interpolation (model.jl:287-306):
+//     Mcₑ averages E_w backward along w onto the primal voxel corners with
+//     weights s∆lₘ and 1/s∆lₑ (isfwdₑ = boundft .!= EE = false);
+//     Mcₘ averages H_w forward along w onto the dual corners with weights
+//     s∆lₑ and 1/s∆lₘ (isfwdₘ = boundft .!= HH = true):
+//         Ec_w[j] = (s∆lₘ[j−1]·E_w[j−1] + s∆lₘ[j]·E_w[j]) / (2·s∆lₑ[j])
+//         Hc_w[j] = (s∆lₑ[j]·H_w[j] + s∆lₑ[j+1]·H_w[j+1]) / (2·s∆lₘ[j]).
+//     Ghosts: E_w[−1] mirrors E_w[0] (weight s∆lₘ[0]) on a symmetry wall,
+//     H_w[N] = 0 there (normal H on the PEC plane); Bloch axes wrap with the
+//     phase e^{∓ikL}.  These are the same two-point means the ε tensor's
+//     off-diagonal averaging uses.
+// All kernels are grid-stride loops over cells, x fastest (coalesced).
+#include <cuda_runtime.h>
+
+#include "operator_common.cuh"
+
+namespace fdfd {
+
+__global__ void k_h_from_e(OpArgs<double> a, Extra<double> ex, const double2 *__restrict__ e,
+                           const double2 *__restrict__ jm, double2 *__restrict__ hout, double2 iow) {
+  const long long nc = a.ncell;
+  for (long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x; cell < nc;
+       cell += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(cell % a.N[0]), j = (int)((cell / a.N[0]) % a.N[1]), k = (int)(cell / ((long long)a.N[0] * a.N[1]));
+    const double2 cmx = a.cm[0][i], cmy = a.cm[1][j], cmz = a.cm[2][k];
+    const double2 ex0 = load_e<double, false>(e, a, ex, i, j, k, 0);
+    const double2 ey0 = load_e<double, false>(e, a, ex, i, j, k, 1);
+    const double2 ez0 = load_e<double, false>(e, a, ex, i, j, k, 2);
+    const double2 exy = load_e<double, false>(e, a, ex, i, j + 1, k, 0);
+    const double2 exz = load_e<double, false>(e, a, ex, i, j, k + 1, 0);
+    const double2 eyx = load_e<double, false>(e, a, ex, i + 1, j, k, 1);
+    const double2 eyz = load_e<double, false>(e, a, ex, i, j, k + 1, 1);
+    const double2 ezx = load_e<double, false>(e, a, ex, i + 1, j, k, 2);
+    const double2 ezy = load_e<double, false>(e, a, ex, i, j + 1, k, 2);
+    double2 h[3];
+    h[0] = csub(cmul(cmy, csub(ezy, ez0)), cmul(cmz, csub(eyz, ey0)));
+    h[1] = csub(cmul(cmz, csub(exz, ex0)), cmul(cmx, csub(ezx, ez0)));
+    h[2] = csub(cmul(cmx, csub(eyx, ey0)), cmul(cmy, csub(exy, ex0)));
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      if (jm) h[c] = cadd(h[c], jm[3 * cell + c]);
+      hout[3 * cell + c] = cmul(iow, h[c]);
+    }
+  }
+}
+
+__global__ void k_corner_mean(OpArgs<double> a, Extra<double> ex, int hfield, const double2 *__restrict__ in,
+                              double2 *__restrict__ out) {
+  const long long nc = a.ncell;
+  for (long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x; cell < nc;
+       cell += (long long)gridDim.x * blockDim.x) {
+    const int g[3] = {(int)(cell % a.N[0]), (int)((cell / a.N[0]) % a.N[1]), (int)(cell / ((long long)a.N[0] * a.N[1]))};
+#pragma unroll
+    for (int w = 0; w < 3; ++w) {
+      const long long stride = (w == 0) ? 1 : (w == 1) ? a.N[0] : (long long)a.N[0] * a.N[1];
+      const int n = a.N[w], t = g[w];
+      const double2 self = in[3 * cell + w];
+      double2 r;
+      if (!hfield) {
+        // backward mean of E_w onto the primal corner t
+        double2 nb, wnb;
+        if (t > 0) {
+          nb = in[3 * (cell - stride) + w];
+          wnb = ex.sdlm[w][t - 1];
+        } else if (a.bloch[w]) {
+          nb = cmul(in[3 * (cell + (long long)(n - 1) * stride) + w], ex.phinv[w]);
+          wnb = ex.sdlm[w][n - 1];
+        } else {
+          nb = self;
+          wnb = ex.sdlm[w][0];
+        }
+        r = cadd(cmul(wnb, nb), cmul(ex.sdlm[w][t], self));
+        r = cmul(r, cinv(cscale(ex.sdle[w][t], 2.0)));
+      } else {
+        // forward mean of H_w onto the dual corner t
+        double2 nb = czero<double2>(), wnb = czero<double2>();
+        if (t + 1 < n) {
+          nb = in[3 * (cell + stride) + w];
+          wnb = ex.sdle[w][t + 1];
+        } else if (a.bloch[w]) {
+          nb = cmul(in[3 * (cell - (long long)(n - 1) * stride) + w], ex.ph[w]);
+          wnb = ex.sdle[w][0];
+        }
+        r = cadd(cmul(ex.sdle[w][t], self), cmul(wnb, nb));
+        r = cmul(r, cinv(cscale(ex.sdlm[w][t], 2.0)));
+      }
+      out[3 * cell + w] = r;
+    }
+  }
+}
+
+int h_from_e_dev_impl(fdfd_handle *h, const double2 *e, const double2 *jm, double2 *hout) {
+  const OpArgs<double> a = op_args<double>(h);
+  const Extra<double> ex = make_extra<double>(h);
+  // i/ω for complex ω
+  const double wr = h->omega[0], wi = h->omega[1], d = wr * wr + wi * wi;
+  if (!(d > 0.0)) return set_error(h, FDFD_ERR_ARG, "h_from_e needs ω ≠ 0");
+  const double2 iow = make_double2(wi / d, wr / d);
+  k_h_from_e<<<152 * 8, 256, 0, h->stream>>>(a, ex, e, jm, hout, iow);
+  h->launches++;
+  return cuda_check(h, cudaGetLastError(), "k_h_from_e");
+}
+
+int corner_mean_dev_impl(fdfd_handle *h, int hfield, const double2 *in, double2 *out) {
+  const OpArgs<double> a = op_args<double>(h);
+  const Extra<double> ex = make_extra<double>(h);
+  k_corner_mean<<<152 * 8, 256, 0, h->stream>>>(a, ex, hfield, in, out);
+  h->launches++;
+  return cuda_check(h, cudaGetLastError(), "k_corner_mean");
+}
+
+}  // namespace fdfd

@@ -517,7 +517,12 @@ int smooth_objects_impl(fdfd_handle *h, const double *const lprim[3], const fdfd
     k_smooth_off<<<152 * 8, 256, 0, st>>>(N0, N1, N2, oc, cax, dobj, eps_bg, h->eoff64, h->smask, dnnz);
   }
   if ((rc = cuda_check(h, cudaGetLastError(), "smoothing kernels"))) return rc;
+  h->has_design = design != nullptr;
   if (design) {
+    for (int a = 0; a < 3; ++a) {
+      h->design_lo[a] = design->lo[a];
+      h->design_hi[a] = design->hi[a];
+    }
     DesignDev dd;
     const long long ne = (long long)(design->hi[0] - design->lo[0]) * (design->hi[1] - design->lo[1]) *
                          (design->hi[2] - design->lo[2]);

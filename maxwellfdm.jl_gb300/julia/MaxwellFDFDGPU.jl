@@ -9,7 +9,7 @@ module MaxwellFDFDGPU
 using LinearAlgebra
 using MaxwellFDFD
 
-export FDFDOperator, create_A_gpu, SolveOpts
+export FDFDOperator, create_A_gpu, SolveOpts, eps_grad, h_from_e, corner_mean
 
 const libfdfd = joinpath(@__DIR__, "..", "libfdfd_gb300.so")
 
@@ -114,15 +114,43 @@ end
 LinearAlgebra.ldiv!(x::Vector{ComplexF64}, A::FDFDOperator, b::Vector{ComplexF64}) = first(solve!(x, A, b))
 Base.:\(A::FDFDOperator, b::Vector{ComplexF64}) = ldiv!(zeros(ComplexF64, length(b)), A, b)
 
-# Adjoint of e = A \ b for a real objective L(e): with g = ∂L/∂e (holomorphic
-# derivative), λ solves transpose(A) λ = g and ∂L/∂b = λ; ∂L/∂A enters through
-# ε (see fdfd_eps_grad).  Written against ChainRulesCore when it is loaded.
+# Adjoint of e = A \ b for a real objective L(e): with g = ∂L/∂e (Wirtinger
+# derivative, dL = 2Re(gᵀde)), λ solves transpose(A) λ = g and ∂L/∂b = λ;
+# ∂L/∂A enters through ε (eps_grad below).  Written against ChainRulesCore
+# when it is loaded.
 function solve_pullback(A::FDFDOperator, e::Vector{ComplexF64}, g::Vector{ComplexF64}; opts::SolveOpts=SolveOpts())
     λ = zeros(ComplexF64, length(g))
     o = SolveOpts(opts.method, opts.precision, opts.tol, opts.maxit, opts.delta, 0, opts.check_every, 1,
                   opts.use_graph)
     solve!(λ, A, g; opts=o)
     return λ
+end
+
+# dL/dε_cc = 2Re(ω²λ_c e_c) at every E_c sample, as a (3, Nx, Ny, Nz) array
+# (component fastest, the DOF order): one transposed solve on the GPU.
+function eps_grad(A::FDFDOperator, e::Vector{ComplexF64}, g::Vector{ComplexF64}; opts::SolveOpts=SolveOpts())
+    grad = zeros(Float64, length(e))
+    st = Ref{SolveStats}()
+    check(ccall((:fdfd_eps_grad, libfdfd), Cint,
+                (Ptr{Cvoid}, Ptr{ComplexF64}, Ptr{ComplexF64}, Ptr{Float64}, Ref{SolveOpts}, Ref{SolveStats}),
+                A.h, e, g, grad, opts, st), A.h)
+    return grad, st[]
+end
+
+# H = (i/ω)(Cₑe + jₘ) — MaxwellFDFD.h_from_e(e, ω, (Pε,Pμ), (Cₑ,Cₘ), (jₑ,jₘ)) with Pμ = I.
+function h_from_e(A::FDFDOperator, e::Vector{ComplexF64}, jₘ::Union{Nothing,Vector{ComplexF64}}=nothing)
+    h = similar(e)
+    check(ccall((:fdfd_h_from_e, libfdfd), Cint, (Ptr{Cvoid}, Ptr{ComplexF64}, Ptr{ComplexF64}, Ptr{ComplexF64}),
+                A.h, e, jₘ === nothing ? C_NULL : jₘ, h), A.h)
+    return h
+end
+
+# Mcₑ*e and Mcₘ*h of MaxwellFDFD.create_Mcs(mdl): fields at the voxel corners.
+function corner_mean(A::FDFDOperator, v::Vector{ComplexF64}; field::Symbol=:E)
+    out = similar(v)
+    check(ccall((:fdfd_corner_mean, libfdfd), Cint, (Ptr{Cvoid}, Int32, Ptr{ComplexF64}, Ptr{ComplexF64}),
+                A.h, field === :E ? 0 : 1, v, out), A.h)
+    return out
 end
 
 end # module

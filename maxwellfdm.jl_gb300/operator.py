@@ -76,6 +76,8 @@ class FDFDOperator:
         self._check(self._lib.fdfd_sync(self._h))
 
     # ---------------------------------------------------------------- material
+    _design_shape = None
+
     def set_eps(self, eps_diag, eps_off=None):
         """eps_diag, eps_off: (Nx,Ny,Nz,3) real arrays (ε_cc at E_c; ε_xy, ε_yz,
         ε_zx at the cell's corner)."""
@@ -109,6 +111,7 @@ class FDFDOperator:
             dd.eps_cells = dptr(keep)
             dptr_ = C.pointer(dd)
         self._check(self._lib.fdfd_smooth_objects(self._h, lp, objs, len(objects), float(eps_bg), dptr_))
+        self._design_shape = None if design is None else tuple(design.hi[a] - design.lo[a] for a in range(3))
 
     def get_eps(self):
         """Returns (eps_diag, eps_off, smask) as (Nx,Ny,Nz,3|4) arrays."""
@@ -182,6 +185,54 @@ class FDFDOperator:
         self._check(self._lib.fdfd_solve_dev(self._h, C.c_void_p(b_ptr), C.c_void_p(x_ptr), C.byref(o),
                                              C.byref(st)))
         return st.as_dict()
+
+    # ---------------------------------------------------------------- fields
+    def h_from_e(self, e, jm=None):
+        """H = (i/ω)·(Cₑ e + jₘ) (h_from_e, model.jl:276-279), as a DOF vector."""
+        e = np.ascontiguousarray(e, dtype=np.complex128).reshape(-1)
+        if e.size != self.n:
+            raise ValueError("e has the wrong length")
+        jmv = None if jm is None else np.ascontiguousarray(jm, dtype=np.complex128).reshape(-1)
+        out = np.empty_like(e)
+        self._check(self._lib.fdfd_h_from_e(self._h, dptr(e), None if jmv is None else dptr(jmv), dptr(out)))
+        return out
+
+    def corner_mean(self, v, field="E"):
+        """create_Mcs corner interpolation (model.jl:287-306): field "E" → Mcₑ v
+        (primal corners), "H" → Mcₘ v (dual corners)."""
+        v = np.ascontiguousarray(v, dtype=np.complex128).reshape(-1)
+        if v.size != self.n:
+            raise ValueError("field vector has the wrong length")
+        f = {"E": _lib.FDFD_EE, "H": _lib.FDFD_HH}[field]
+        out = np.empty_like(v)
+        self._check(self._lib.fdfd_corner_mean(self._h, f, dptr(v), dptr(out)))
+        return out
+
+    # ---------------------------------------------------------------- adjoint
+    def eps_grad(self, e, g, tol=1e-8, precision="fp64", maxit=200000, delta=0.1, check_every=50, use_graph=True):
+        """dL/dε_cc at every E_c sample for A e = b and g = ∂L/∂e (Wirtinger
+        derivative, dL = 2·Re(gᵀ de)): solves Aᵀ λ = g on the GPU and returns
+        2·Re(ω²·λ·e) as an (Nx,Ny,Nz,3) array, with the solve's stats."""
+        e = np.ascontiguousarray(e, dtype=np.complex128).reshape(-1)
+        g = np.ascontiguousarray(g, dtype=np.complex128).reshape(-1)
+        if e.size != self.n or g.size != self.n:
+            raise ValueError("e and g need 3·Ncell entries")
+        grad = np.empty(self.n)
+        o = self._opts(tol, precision, "bicgstab", maxit, False, delta, check_every, True, use_graph)
+        st = _lib.fdfd_stats()
+        self._check(self._lib.fdfd_eps_grad(self._h, dptr(e), dptr(g), dptr(grad), C.byref(o), C.byref(st)))
+        return _aos_cell(grad, self.N, 3), st.as_dict()
+
+    def design_grad(self, grad):
+        """Chain dL/dε_ww ((Nx,Ny,Nz,3), as eps_grad returns it) to the cells
+        of the design region applied by smooth_objects → (hi−lo) array."""
+        if self._design_shape is None:
+            raise ValueError("no design region was applied")
+        gv = _cell_aos(grad, self.N, np.float64)
+        ds = self._design_shape
+        out = np.empty(ds[0] * ds[1] * ds[2])
+        self._check(self._lib.fdfd_design_grad(self._h, dptr(gv), dptr(out)))
+        return np.transpose(out.reshape(ds[2], ds[1], ds[0]), (2, 1, 0))
 
     def _opts(self, tol, precision, method, maxit, x0_given, delta, check_every, transpose, use_graph):
         return _lib.default_opts(

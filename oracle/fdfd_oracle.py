@@ -478,6 +478,55 @@ def h_from_e(e, omega, Ce, jm_vec=None):
     return (1j / omega) * t
 
 
+def create_Mcs(grid, sdl_e, sdl_m, kbloch=(0.0, 0.0, 0.0)):
+    """Corner interpolation (create_Mcs, model.jl:287-306), restated from
+    the roles given there — create_mean(isfwd, ∆l, ∆l′⁻¹): the mean of each
+    component along its own axis, weighted by ∆l and scaled by ∆l′⁻¹/2:
+      Mcₑ (isfwdₑ = boundft .!= EE = false, ∆l = s∆lₘ, ∆l′⁻¹ = 1/s∆lₑ):
+          Ec_w[j] = (s∆lₘ[j−1]·E_w[j−1] + s∆lₘ[j]·E_w[j]) / (2·s∆lₑ[j])
+      Mcₘ (isfwdₘ = boundft .!= HH = true, ∆l = s∆lₑ, ∆l′⁻¹ = 1/s∆lₘ):
+          Hc_w[j] = (s∆lₑ[j]·H_w[j] + s∆lₑ[j+1]·H_w[j+1]) / (2·s∆lₘ[j])
+    Ghosts as in the operator: E_w[−1] = E_w[0] with weight s∆lₘ[0] on a
+    symmetry wall (the ε averaging's mirror), H_w[N] = 0 there; Bloch axes
+    wrap with the phase e^{∓ikL}.  MaxwellBase's create_mean itself is not
+    available here, so parity with it is unpinned."""
+    N = grid.N
+    n = 3 * grid.ncell
+    ph = _bloch_phase(grid, kbloch)
+    I, J, K = _ijk(N)
+    idx = (I, J, K)
+    ce, cm = _Coo(n), _Coo(n)
+    for w in range(3):
+        rows = _dof(w, I, J, K, N)
+        t = idx[w]
+        # E: backward
+        inv = 1.0 / (2.0 * sdl_e[w][t])
+        ce.add(rows, rows, sdl_m[w][t] * inv)
+        nb = [I.copy(), J.copy(), K.copy()]
+        g = t == 0
+        if grid.isbloch[w]:
+            nb[w] = np.where(g, N[w] - 1, t - 1)
+            fac = np.where(g, 1.0 / ph[w], 1.0)
+        else:
+            nb[w] = np.where(g, 0, t - 1)
+            fac = np.ones(I.shape, dtype=np.complex128)
+        ce.add(rows, _dof(w, nb[0], nb[1], nb[2], N), sdl_m[w][nb[w]] * inv * fac)
+        # H: forward
+        inv = 1.0 / (2.0 * sdl_m[w][t])
+        cm.add(rows, rows, sdl_e[w][t] * inv)
+        nb = [I.copy(), J.copy(), K.copy()]
+        g = t == N[w] - 1
+        if grid.isbloch[w]:
+            nb[w] = np.where(g, 0, t + 1)
+            cm.add(rows, _dof(w, nb[0], nb[1], nb[2], N), sdl_e[w][nb[w]] * inv * np.where(g, ph[w], 1.0))
+        else:
+            keep = ~g
+            nb[w] = np.where(g, 0, t + 1)
+            val = sdl_e[w][nb[w]] * inv
+            cm.add(rows[keep], _dof(w, nb[0], nb[1], nb[2], N)[keep], val[keep])
+    return ce.csr(), cm.csr()
+
+
 # --------------------------------------------------------------------------
 # Material assignment and Kottke smoothing (src/model/full.jl:16-70)
 # --------------------------------------------------------------------------
@@ -812,6 +861,19 @@ class System:
 
     def b(self):
         return create_b(self.omega, field_to_vec(self.je))
+
+
+def adjoint_eps_grad(A, omega, e, g):
+    """dL/dε_cc at every E_c sample, (3·Ncell,) real, for A e = b and the
+    Wirtinger derivative g = ∂L/∂e (dL = 2·Re(gᵀ de)).  A = K − ω²·Pε
+    (create_A, src/model/model.jl:238-259) gives ∂A/∂ε_cc = −ω² on the
+    diagonal, hence de/dε_cc = ω²·A⁻¹(e_c u_c) and
+    dL/dε_cc = 2·Re(ω²·λ_c·e_c) with Aᵀλ = g.  The reference has no adjoint;
+    this restates the derivative of the operator it assembles.  Direct
+    solve (small systems only)."""
+    import scipy.sparse.linalg as spla
+    lam = spla.spsolve(A.T.tocsc(), g)
+    return 2.0 * np.real(omega ** 2 * lam * e), lam
 
 
 # --------------------------------------------------------------------------
