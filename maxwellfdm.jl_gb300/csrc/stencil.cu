@@ -193,20 +193,25 @@ struct EoffSrc {
 };
 
 // x- and y-directed corner terms of plane k (E(k−1), E(k) in slots sm, s0).
-// A thread owns xc/yc positions tid and tid + NTHR; all its ε loads are
-// issued before any is used, so their latencies overlap.
+// A thread owns xc/yc positions t and t + NTHR; all its ε loads are issued
+// before any is used, so their latencies overlap.  The positions beyond
+// NTHR (8 of xc, 32 of yc) go to threads other than those that computed the
+// 41 halo positions of H, so no thread does more than one extra round.
+constexpr int H_EXTRA = (TX + 1) * (TY + 1) - NTHR;        // 41
+constexpr int XC_EXTRA = TY * (TX + 1) - NTHR;              // 8
 template <typename R, typename ET>
 __device__ __forceinline__ void stage_xy(const ET &E, OffTile<R> &O, const CoefTile<R> &T, const OpArgs<R> &a,
                                          const EoffSrc<R> &src, int i0, int j0, int k, int sm, int s0, int tid) {
   using C = typename CT<R>::C;
   constexpr int NXC = TY * (TX + 1), NYC = (TY + 1) * TX;
+  const int tx0 = (tid + NTHR - H_EXTRA) % NTHR, ty0 = (tid + NTHR - H_EXTRA - XC_EXTRA) % NTHR;
   R vx[2][2], vy[2][2];
 #pragma unroll
   for (int r = 0; r < 2; ++r) {
-    const int p = tid + r * NTHR;
     vx[r][0] = vx[r][1] = vy[r][0] = vy[r][1] = R(0);
     {
       // corners no active output reads (beyond the one-past corner) stay 0
+      const int p = tx0 + r * NTHR;
       const int ii = p % (TX + 1), jj = p / (TX + 1);
       if (p < NXC && i0 + ii <= a.N[0] && j0 + jj < a.N[1]) {
         vx[r][0] = src.get(a, 0, i0, j0, ii, jj, k);
@@ -214,6 +219,7 @@ __device__ __forceinline__ void stage_xy(const ET &E, OffTile<R> &O, const CoefT
       }
     }
     {
+      const int p = ty0 + r * NTHR;
       const int ii = p % TX, jj = p / TX;
       if (p < NYC && i0 + ii < a.N[0] && j0 + jj <= a.N[1]) {
         vy[r][0] = src.get(a, 0, i0, j0, ii, jj, k);
@@ -224,15 +230,16 @@ __device__ __forceinline__ void stage_xy(const ET &E, OffTile<R> &O, const CoefT
   const C wmz = a.wm[2][k], wpz = a.wp[2][k];
 #pragma unroll
   for (int r = 0; r < 2; ++r) {
-    const int p = tid + r * NTHR;
+    const int p = tx0 + r * NTHR;
     if (p < NXC) {
       const int ii = p % (TX + 1), jj = p / (TX + 1);
       const C ay = cadd(cmul(T.wmy[jj + 1], E.get(s0, 1, jj - 1, ii)), cmul(T.wpy[jj + 1], E.get(s0, 1, jj, ii)));
       const C az = cadd(cmul(wmz, E.get(sm, 2, jj, ii)), cmul(wpz, E.get(s0, 2, jj, ii)));
       O.xc[jj][ii] = cadd(cscale(ay, vx[r][0]), cscale(az, vx[r][1]));
     }
-    if (p < NYC) {
-      const int ii = p % TX, jj = p / TX;
+    const int q = ty0 + r * NTHR;
+    if (q < NYC) {
+      const int ii = q % TX, jj = q / TX;
       const C ax = cadd(cmul(T.wmx[ii + 1], E.get(s0, 0, jj, ii - 1)), cmul(T.wpx[ii + 1], E.get(s0, 0, jj, ii)));
       const C az = cadd(cmul(wmz, E.get(sm, 2, jj, ii)), cmul(wpz, E.get(s0, 2, jj, ii)));
       O.yc[jj][ii] = cadd(cscale(ax, vy[r][0]), cscale(az, vy[r][1]));
@@ -422,11 +429,12 @@ __global__ void __launch_bounds__(NTHR) k_apply(OpArgs<R> a, Extra<R> ex, const 
       stage_z<R>(S.E, S.O, S.T, a, g, i0, j0, k + 1, s1, tid);
     }
     zvalid = offd;
-    __syncthreads();
+    __syncthreads();  // H(k), staged corners complete; nobody reads E(k−1) any more
     if (active)
       output_cell<R, EPI, TRANSPOSE>(S.E, S.H, S.T, S.O, a, ex, pf, x, y, gi, gj, k, tx, ty, sm, s0, s1, hc, hp,
                                      offd, acc);
-    __syncthreads();  // everyone done with E(k−1) and H(k−1)
+    // E(k−1)'s slot takes E(k+2); the next iteration's first barrier orders
+    // it (and this plane's reads of H and the corners) before their reuse
     if (k + 1 < k1) load_plane<R, TRANSPOSE>(S.E, a, ex, x, i0, j0, k + 2, sm, tid);
   }
   if (EPI != EPI_STORE) {
@@ -614,10 +622,10 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2)
       stage_z<R>(E, O, T, a, e1, i0, j0, k + 1, s1, tid);
     }
     zvalid = offd;
-    __syncthreads();
-    if (active)
-      output_cell<R, EPI, false>(E, H, T, O, a, ex, pf, x, y, gi, gj, k, tx, ty, sm, s0, s1, hc, hp, offd, acc);
-    __syncthreads();  // slot of E(k−1) is free
+    __syncthreads();  // H(k), staged corners complete; nobody reads E(k−1) any more
+    // refill E(k−1)'s slot (and its ε slot) right away: the output stage reads
+    // only E(k), H and the staged corners, and the next iteration's first
+    // barrier orders this plane's reads of H/corners before they are rewritten
     if (tid == 0) {
       const int q = k + 3;
       if (q <= k1) {
@@ -625,6 +633,8 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2)
         issue_plane<R>(smraw, bars, &tmap, &emap, a, ex, tilecol, cx, cy, i0, j0, k0, q, sm);
       }
     }
+    if (active)
+      output_cell<R, EPI, false>(E, H, T, O, a, ex, pf, x, y, gi, gj, k, tx, ty, sm, s0, s1, hc, hp, offd, acc);
   }
   if (!ok) {
     // a bounded wait gave up (warp 0 only): report it and drain this
