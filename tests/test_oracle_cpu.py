@@ -189,3 +189,22 @@ def test_bench_replicas_max_over_ranks():
     for p in ps:
         p.join(timeout=60)
     assert out == {0: 2.5, 1: 2.5}
+
+
+def test_native_csr_baseline_matches_oracle(oracle):
+    """The OpenMP CSR SpMV/BiCGSTAB (the benchmark's CPU baseline) against
+    scipy and the oracle's own BiCGSTAB on the same assembled A."""
+    from oracle.csr_native import NativeCSR
+    O = oracle
+    g = O.uniform_grid((10, 9, 8))
+    S = O.System(g, 2 * np.pi / 6.0, ((2, 2, 2), (2, 2, 2)), [O.Sphere((5.1, 4.2, 3.9), 2.2, 6.0)])
+    S.add_pointsrc((4.6, 4.5, 4.0), (0.2, 0.1, 1.0))
+    b = S.b()
+    M = NativeCSR(S.A, threads=2)
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal(b.size) + 1j * rng.standard_normal(b.size)
+    assert np.max(np.abs(M.matvec(x) - S.A @ x)) <= 1e-13 * np.max(np.abs(S.A @ x))
+    xo, ito, _ = O.bicgstab(S.A, b, tol=1e-8, maxit=5000)
+    xn, itn, rel = M.bicgstab(b, tol=1e-8, maxit=5000)
+    assert rel < 1e-8 and abs(itn - ito) <= max(3, ito // 20), (itn, ito)
+    assert np.linalg.norm(b - S.A @ xn) / np.linalg.norm(b) < 1e-7
