@@ -38,12 +38,24 @@ namespace fdfd {
 constexpr int EX = TX + 2, EY = TY + 2;  // E tile with halo: −1 … T
 constexpr int HX = TX + 1, HY = TY + 1;  // H tile: −1 … T−1
 
+// H of the current plane over the tile and its low halo (−1 … T−1).  Each
+// thread also keeps the H it computed at its own cell in registers, for
+// this plane and the previous one, so only the neighbours' values (i−1 and
+// j−1) are read back from here.
 template <typename R>
 struct HTile {
   using C = typename CT<R>::C;
-  C hx[2][HY][HX];
-  C hy[2][HY][HX];
+  C hx[HY][HX];
+  C hy[HY][HX];
   C hz[HY][HX];
+};
+
+// Values a thread carries from the H stage to the output stage of a plane:
+// H and E at its own cell.
+template <typename R>
+struct Own {
+  using C = typename CT<R>::C;
+  C hx, hy, hz, ex, ey, ez;
 };
 
 // Per-tile copies of the x and y coefficient arrays, indexed by position+1
@@ -152,22 +164,47 @@ __device__ __forceinline__ void fill_coef(CoefTile<R> &T, const OpArgs<R> &a, in
   }
 }
 
-// H(k) = Cₑ E over the tile positions −1 … T−1 in x and y.
+// H = Cₑ E at tile position (ii, jj) of plane k (E(k), E(k+1) in slots sk,
+// sk1); also returns E(k) there.
+template <typename R, typename ET>
+__device__ __forceinline__ void curl_e(const ET &E, const CoefTile<R> &T, typename CT<R>::C cmz, int sk, int sk1,
+                                       int ii, int jj, Own<R> &o) {
+  using C = typename CT<R>::C;
+  const C cmx = T.cmx[ii + 1];
+  const C cmy = T.cmy[jj + 1];
+  o.ex = E.get(sk, 0, jj, ii);
+  o.ey = E.get(sk, 1, jj, ii);
+  o.ez = E.get(sk, 2, jj, ii);
+  const C exy = E.get(sk, 0, jj + 1, ii), exz = E.get(sk1, 0, jj, ii);
+  const C eyx = E.get(sk, 1, jj, ii + 1), eyz = E.get(sk1, 1, jj, ii);
+  const C ezx = E.get(sk, 2, jj, ii + 1), ezy = E.get(sk, 2, jj + 1, ii);
+  o.hx = csub(cmul(cmy, csub(ezy, o.ez)), cmul(cmz, csub(eyz, o.ey)));
+  o.hy = csub(cmul(cmz, csub(exz, o.ex)), cmul(cmx, csub(ezx, o.ez)));
+  o.hz = csub(cmul(cmx, csub(eyx, o.ey)), cmul(cmy, csub(exy, o.ex)));
+}
+
+constexpr int H_HALO = TX + TY;  // halo positions: column i = −1 (TY), row j = −1 (TX)
+
+// H(k): every thread at its own cell (kept in `own` and stored for its
+// neighbours), threads 0 … TX+TY−1 also at one low-halo position, storing
+// only the components a neighbour reads there (hy, hz on the i = −1
+// column; hx, hz on the j = −1 row).
 template <typename R, typename ET>
 __device__ __forceinline__ void compute_h(const ET &E, HTile<R> &H, const CoefTile<R> &T, const OpArgs<R> &a,
-                                          int k, int sk, int sk1, int hslot, int tid) {
+                                          int k, int sk, int sk1, int tx, int ty, int tid, Own<R> &own) {
   using C = typename CT<R>::C;
   const C cmz = a.cm[2][cidx(a, 2, k)];
-  for (int p = tid; p < HX * HY; p += NTHR) {
-    const int ii = p % HX - 1, jj = p / HX - 1;
-    const C cmx = T.cmx[ii + 1];
-    const C cmy = T.cmy[jj + 1];
-    const C ex0 = E.get(sk, 0, jj, ii), exy = E.get(sk, 0, jj + 1, ii), exz = E.get(sk1, 0, jj, ii);
-    const C ey0 = E.get(sk, 1, jj, ii), eyx = E.get(sk, 1, jj, ii + 1), eyz = E.get(sk1, 1, jj, ii);
-    const C ez0 = E.get(sk, 2, jj, ii), ezx = E.get(sk, 2, jj, ii + 1), ezy = E.get(sk, 2, jj + 1, ii);
-    H.hx[hslot][jj + 1][ii + 1] = csub(cmul(cmy, csub(ezy, ez0)), cmul(cmz, csub(eyz, ey0)));
-    H.hy[hslot][jj + 1][ii + 1] = csub(cmul(cmz, csub(exz, ex0)), cmul(cmx, csub(ezx, ez0)));
-    H.hz[jj + 1][ii + 1] = csub(cmul(cmx, csub(eyx, ey0)), cmul(cmy, csub(exy, ex0)));
+  curl_e<R>(E, T, cmz, sk, sk1, tx, ty, own);
+  H.hx[ty + 1][tx + 1] = own.hx;
+  H.hy[ty + 1][tx + 1] = own.hy;
+  H.hz[ty + 1][tx + 1] = own.hz;
+  if (tid < H_HALO) {
+    const int ii = tid < TY ? -1 : tid - TY, jj = tid < TY ? tid : -1;
+    Own<R> h;
+    curl_e<R>(E, T, cmz, sk, sk1, ii, jj, h);
+    if (ii < 0) H.hy[jj + 1][0] = h.hy;
+    else H.hx[0][ii + 1] = h.hx;
+    H.hz[jj + 1][ii + 1] = h.hz;
   }
 }
 
@@ -195,16 +232,16 @@ struct EoffSrc {
 // x- and y-directed corner terms of plane k (E(k−1), E(k) in slots sm, s0).
 // A thread owns xc/yc positions t and t + NTHR; all its ε loads are issued
 // before any is used, so their latencies overlap.  The positions beyond
-// NTHR (8 of xc, 32 of yc) go to threads other than those that computed the
-// 41 halo positions of H, so no thread does more than one extra round.
-constexpr int H_EXTRA = (TX + 1) * (TY + 1) - NTHR;        // 41
-constexpr int XC_EXTRA = TY * (TX + 1) - NTHR;              // 8
+// NTHR (8 of xc, 32 of yc) go to warps 2 and 3, clear of the two warps that
+// computed the H halo, so no warp does more than one extra round.
+constexpr int XC_ROT = 2 * TX;                              // xc extras → warp 2
+constexpr int YC_ROT = 3 * TX;                              // yc extras → warp 3
 template <typename R, typename ET>
 __device__ __forceinline__ void stage_xy(const ET &E, OffTile<R> &O, const CoefTile<R> &T, const OpArgs<R> &a,
                                          const EoffSrc<R> &src, int i0, int j0, int k, int sm, int s0, int tid) {
   using C = typename CT<R>::C;
   constexpr int NXC = TY * (TX + 1), NYC = (TY + 1) * TX;
-  const int tx0 = (tid + NTHR - H_EXTRA) % NTHR, ty0 = (tid + NTHR - H_EXTRA - XC_EXTRA) % NTHR;
+  const int tx0 = (tid + NTHR - XC_ROT) % NTHR, ty0 = (tid + NTHR - YC_ROT) % NTHR;
   R vx[2][2], vy[2][2];
 #pragma unroll
   for (int r = 0; r < 2; ++r) {
@@ -292,19 +329,19 @@ __device__ __forceinline__ void prefetch(Pre<R> &pf, const OpArgs<R> &a, const t
 }
 
 // y(k) at the thread's cell (gi, gj, k) from shared memory.
-template <typename R, int EPI, bool TRANSPOSE, typename ET>
-__device__ __forceinline__ void output_cell(const ET &E, const HTile<R> &H, const CoefTile<R> &T,
-                                            const OffTile<R> &O, const OpArgs<R> &a, const Extra<R> &ex,
-                                            const Pre<R> &pf,
+template <typename R, int EPI, bool TRANSPOSE>
+__device__ __forceinline__ void output_cell(const HTile<R> &H, const CoefTile<R> &T, const OffTile<R> &O,
+                                            const OpArgs<R> &a, const Extra<R> &ex, const Pre<R> &pf,
+                                            const Own<R> &own, typename CT<R>::C hxkm, typename CT<R>::C hykm,
                                             const typename CT<R>::C *__restrict__ x,
                                             typename CT<R>::C *__restrict__ y, int gi, int gj, int k, int tx, int ty,
-                                            int sm, int s0, int s1, int hc, int hp, bool offd, Accs<R> &acc) {
+                                            bool offd, Accs<R> &acc) {
   using C = typename CT<R>::C;
   const C cez = a.ce[2][k];
   const C cex = T.cex[tx + 1], cey = T.cey[ty + 1];
-  const C hz00 = H.hz[ty + 1][tx + 1], hzjm = H.hz[ty][tx + 1], hzim = H.hz[ty + 1][tx];
-  const C hyk = H.hy[hc][ty + 1][tx + 1], hykm = H.hy[hp][ty + 1][tx + 1], hyim = H.hy[hc][ty + 1][tx];
-  const C hxk = H.hx[hc][ty + 1][tx + 1], hxkm = H.hx[hp][ty + 1][tx + 1], hxjm = H.hx[hc][ty][tx + 1];
+  const C hz00 = own.hz, hzjm = H.hz[ty][tx + 1], hzim = H.hz[ty + 1][tx];
+  const C hyk = own.hy, hyim = H.hy[ty + 1][tx];
+  const C hxk = own.hx, hxjm = H.hx[ty][tx + 1];
   C yx = csub(cmul(cey, csub(hz00, hzjm)), cmul(cez, csub(hyk, hykm)));
   C yy = csub(cmul(cez, csub(hxk, hxkm)), cmul(cex, csub(hz00, hzim)));
   C yz = csub(cmul(cex, csub(hyk, hyim)), cmul(cey, csub(hxk, hxjm)));
@@ -318,7 +355,7 @@ __device__ __forceinline__ void output_cell(const ET &E, const HTile<R> &H, cons
   const bool pinz = pin_yx || pin_xy;
   // the cell's own values: shared memory holds 0 for pinned DOFs (they do
   // not enter the curl), but the ε term uses the true value
-  C e_x = E.get(s0, 0, ty, tx), e_y = E.get(s0, 1, ty, tx), e_z = E.get(s0, 2, ty, tx);
+  C e_x = own.ex, e_y = own.ey, e_z = own.ez;
   if (pinx) e_x = own_e<R, TRANSPOSE>(x, ex, cell, 0, gi, gj, k);
   if (piny) e_y = own_e<R, TRANSPOSE>(x, ex, cell, 1, gi, gj, k);
   if (pinz) e_z = own_e<R, TRANSPOSE>(x, ex, cell, 2, gi, gj, k);
@@ -385,7 +422,7 @@ __device__ __forceinline__ bool offd_on(const OpArgs<double> &a, long long tilec
 
 // ------------------------------------------------------------------ plain kernel
 template <typename R, int EPI, bool TRANSPOSE>
-__global__ void __launch_bounds__(NTHR) k_apply(OpArgs<R> a, Extra<R> ex, const typename CT<R>::C *__restrict__ x,
+__global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2) k_apply(OpArgs<R> a, Extra<R> ex, const typename CT<R>::C *__restrict__ x,
                                                 typename CT<R>::C *__restrict__ y,
                                                 const typename CT<R>::C *__restrict__ aux0, RedBuf red, int fin,
                                                 KScalars *sc) {
@@ -411,16 +448,24 @@ __global__ void __launch_bounds__(NTHR) k_apply(OpArgs<R> a, Extra<R> ex, const 
   load_plane<R, TRANSPOSE>(S.E, a, ex, x, i0, j0, k0, k0 % 3, tid);
   load_plane<R, TRANSPOSE>(S.E, a, ex, x, i0, j0, k0 + 1, (k0 + 1) % 3, tid);
   __syncthreads();
-  compute_h<R>(S.E, S.H, S.T, a, k0 - 1, (k0 + 2) % 3, k0 % 3, (k0 + 1) & 1, tid);
+  // H(k0−1) at the thread's own cell (the output of plane k0 reads no
+  // neighbour of it)
+  typename CT<R>::C hxp, hyp;
+  {
+    Own<R> o;
+    curl_e<R>(S.E, S.T, a.cm[2][cidx(a, 2, k0 - 1)], (k0 + 2) % 3, k0 % 3, tx, ty, o);
+    hxp = o.hx;
+    hyp = o.hy;
+  }
   bool zvalid = false;  // zc[k & 1] already holds plane k's z-directed corners
 
   for (int k = k0; k < k1; ++k) {
     const int sm = (k + 2) % 3, s0 = k % 3, s1 = (k + 1) % 3;
-    const int hc = k & 1, hp = (k + 1) & 1;
     Pre<R> pf;
     if (active) prefetch<R, EPI>(pf, a, aux0, gi + (long long)a.N[0] * (gj + (long long)a.N[1] * k));
-    __syncthreads();  // E(k+1) present, H(k−1) complete
-    compute_h<R>(S.E, S.H, S.T, a, k, s0, s1, hc, tid);
+    __syncthreads();  // E(k+1) present; the previous plane's reads of H are done
+    Own<R> own;
+    compute_h<R>(S.E, S.H, S.T, a, k, s0, s1, tx, ty, tid, own);
     const bool offd = offd_on(a, tilecol, k);
     if (offd) {
       const EoffSrc<R> g{nullptr};
@@ -430,9 +475,9 @@ __global__ void __launch_bounds__(NTHR) k_apply(OpArgs<R> a, Extra<R> ex, const 
     }
     zvalid = offd;
     __syncthreads();  // H(k), staged corners complete; nobody reads E(k−1) any more
-    if (active)
-      output_cell<R, EPI, TRANSPOSE>(S.E, S.H, S.T, S.O, a, ex, pf, x, y, gi, gj, k, tx, ty, sm, s0, s1, hc, hp,
-                                     offd, acc);
+    if (active) output_cell<R, EPI, TRANSPOSE>(S.H, S.T, S.O, a, ex, pf, own, hxp, hyp, x, y, gi, gj, k, tx, ty, offd, acc);
+    hxp = own.hx;
+    hyp = own.hy;
     // E(k−1)'s slot takes E(k+2); the next iteration's first barrier orders
     // it (and this plane's reads of H and the corners) before their reuse
     if (k + 1 < k1) load_plane<R, TRANSPOSE>(S.E, a, ex, x, i0, j0, k + 2, sm, tid);
@@ -596,13 +641,20 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2)
     pin_fixup<R>(E, 1, i0, j0, k0, tid);
     __syncthreads();
   }
-  compute_h<R>(E, H, T, a, kfirst, 0, 1, (k0 + 1) & 1, tid);
+  // H(k0−1) at the thread's own cell (the output of plane k0 reads no
+  // neighbour of it)
+  typename CT<R>::C hxp, hyp;
+  {
+    Own<R> o;
+    curl_e<R>(E, T, a.cm[2][cidx(a, 2, kfirst)], 0, 1, tx, ty, o);
+    hxp = o.hx;
+    hyp = o.hy;
+  }
   bool zvalid = false;  // zc[k & 1] already holds plane k's z-directed corners
 
   for (int k = k0; k < k1; ++k) {
     const int pm = k - 1 - kfirst, p0 = k - kfirst, p1 = k + 1 - kfirst;
     const int sm = pm % G::NSLOT, s0 = p0 % G::NSLOT, s1 = p1 % G::NSLOT;
-    const int hc = k & 1, hp = (k + 1) & 1;
     Pre<R> pf;
     if (active) prefetch<R, EPI>(pf, a, aux0, gi + (long long)a.N[0] * (gj + (long long)a.N[1] * k));
     if (warp0) ok = mbar_wait(smem_u32(&bars[s1]), (p1 / G::NSLOT) & 1) && ok;
@@ -610,8 +662,9 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2)
       __syncthreads();
       pin_fixup<R>(E, s1, i0, j0, k + 1, tid);
     }
-    __syncthreads();  // E(k+1) present and fixed up, H(k−1) complete
-    compute_h<R>(E, H, T, a, k, s0, s1, hc, tid);
+    __syncthreads();  // E(k+1) present and fixed up; the previous plane's reads of H are done
+    Own<R> own;
+    compute_h<R>(E, H, T, a, k, s0, s1, tx, ty, tid, own);
     const bool offd = offd_on(a, tilecol, k);
     if (offd) {
       const bool eo = G::EO_SLOT > 0 && ex.eoff_tma;
@@ -633,8 +686,9 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2)
         issue_plane<R>(smraw, bars, &tmap, &emap, a, ex, tilecol, cx, cy, i0, j0, k0, q, sm);
       }
     }
-    if (active)
-      output_cell<R, EPI, false>(E, H, T, O, a, ex, pf, x, y, gi, gj, k, tx, ty, sm, s0, s1, hc, hp, offd, acc);
+    if (active) output_cell<R, EPI, false>(H, T, O, a, ex, pf, own, hxp, hyp, x, y, gi, gj, k, tx, ty, offd, acc);
+    hxp = own.hx;
+    hyp = own.hy;
   }
   if (!ok) {
     // a bounded wait gave up (warp 0 only): report it and drain this
