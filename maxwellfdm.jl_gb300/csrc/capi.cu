@@ -370,6 +370,22 @@ int fdfd_create(const fdfd_desc *d, fdfd_handle **out) {
       }
     }
   }
+  // the contiguous index range (outside the PML) where the curl and averaging
+  // coefficients are real: operator tiles inside it take a real-arithmetic path
+  for (int w = 0; w < 3; ++w) {
+    const int N = h->N[w];
+    auto is_real = [&](int i) {
+      for (int kd = 0; kd < 4; ++kd)
+        if (c64[(size_t)kd * st + h->coef_off[w] + i].y != 0.0) return false;
+      return true;
+    };
+    int lo = 0;
+    while (lo < N && !is_real(lo)) ++lo;
+    int hi = lo;
+    while (hi + 1 < N && is_real(hi + 1)) ++hi;
+    h->rlo[w] = lo < N ? lo : 1;
+    h->rhi[w] = lo < N ? hi : 0;
+  }
   if (cudaMalloc(&h->coef64, c64.size() * sizeof(double2)) != cudaSuccess ||
       cudaMalloc(&h->coef32, c32.size() * sizeof(float2)) != cudaSuccess) {
     cudaGetLastError();

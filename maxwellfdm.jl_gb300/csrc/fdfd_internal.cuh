@@ -57,6 +57,7 @@ struct OpArgs {
   const R *eoff;     // 3*ncell (SoA) or nullptr
   const uint8_t *oflag;  // per (tile, z-plane) flag: off-diagonal present; nullptr = everywhere
   C w2;              // ω²
+  int rlo[3], rhi[3];  // per axis: index range whose cm, ce, wm, wp are all real (outside the PML)
 };
 
 // Epilogue of the stencil: what to do with y = A x at each cell.
@@ -108,6 +109,7 @@ struct fdfd_handle {
   float2 *coef32 = nullptr;
   long long coef_off[3] = {0, 0, 0};
   int coef_stride = 0;  // = N[0]+N[1]+N[2]
+  int rlo[3] = {1, 1, 1}, rhi[3] = {0, 0, 0};  // real-coefficient index range per axis (empty: lo > hi)
   double *eps64 = nullptr;
   float *eps32 = nullptr;
   double *eoff64 = nullptr;

@@ -166,7 +166,14 @@ __device__ __forceinline__ void fill_coef(CoefTile<R> &T, const OpArgs<R> &a, in
 
 // H = Cₑ E at tile position (ii, jj) of plane k (E(k), E(k+1) in slots sk,
 // sk1); also returns E(k) there.
-template <typename R, typename ET>
+// c·v for a coefficient c that is real when RC (tiles outside the PML)
+template <bool RC, typename C>
+__device__ __forceinline__ C mulc(C c, C v) {
+  if constexpr (RC) return cscale(v, c.x);
+  else return cmul(c, v);
+}
+
+template <typename R, bool RC, typename ET>
 __device__ __forceinline__ void curl_e(const ET &E, const CoefTile<R> &T, typename CT<R>::C cmz, int sk, int sk1,
                                        int ii, int jj, Own<R> &o) {
   using C = typename CT<R>::C;
@@ -178,9 +185,9 @@ __device__ __forceinline__ void curl_e(const ET &E, const CoefTile<R> &T, typena
   const C exy = E.get(sk, 0, jj + 1, ii), exz = E.get(sk1, 0, jj, ii);
   const C eyx = E.get(sk, 1, jj, ii + 1), eyz = E.get(sk1, 1, jj, ii);
   const C ezx = E.get(sk, 2, jj, ii + 1), ezy = E.get(sk, 2, jj + 1, ii);
-  o.hx = csub(cmul(cmy, csub(ezy, o.ez)), cmul(cmz, csub(eyz, o.ey)));
-  o.hy = csub(cmul(cmz, csub(exz, o.ex)), cmul(cmx, csub(ezx, o.ez)));
-  o.hz = csub(cmul(cmx, csub(eyx, o.ey)), cmul(cmy, csub(exy, o.ex)));
+  o.hx = csub(mulc<RC>(cmy, csub(ezy, o.ez)), mulc<RC>(cmz, csub(eyz, o.ey)));
+  o.hy = csub(mulc<RC>(cmz, csub(exz, o.ex)), mulc<RC>(cmx, csub(ezx, o.ez)));
+  o.hz = csub(mulc<RC>(cmx, csub(eyx, o.ey)), mulc<RC>(cmy, csub(exy, o.ex)));
 }
 
 constexpr int H_HALO = TX + TY;  // halo positions: column i = −1 (TY), row j = −1 (TX)
@@ -189,19 +196,19 @@ constexpr int H_HALO = TX + TY;  // halo positions: column i = −1 (TY), row j 
 // neighbours), threads 0 … TX+TY−1 also at one low-halo position, storing
 // only the components a neighbour reads there (hy, hz on the i = −1
 // column; hx, hz on the j = −1 row).
-template <typename R, typename ET>
+template <typename R, bool RC, typename ET>
 __device__ __forceinline__ void compute_h(const ET &E, HTile<R> &H, const CoefTile<R> &T, const OpArgs<R> &a,
                                           int k, int sk, int sk1, int tx, int ty, int tid, Own<R> &own) {
   using C = typename CT<R>::C;
   const C cmz = a.cm[2][cidx(a, 2, k)];
-  curl_e<R>(E, T, cmz, sk, sk1, tx, ty, own);
+  curl_e<R, RC>(E, T, cmz, sk, sk1, tx, ty, own);
   H.hx[ty + 1][tx + 1] = own.hx;
   H.hy[ty + 1][tx + 1] = own.hy;
   H.hz[ty + 1][tx + 1] = own.hz;
   if (tid < H_HALO) {
     const int ii = tid < TY ? -1 : tid - TY, jj = tid < TY ? tid : -1;
     Own<R> h;
-    curl_e<R>(E, T, cmz, sk, sk1, ii, jj, h);
+    curl_e<R, RC>(E, T, cmz, sk, sk1, ii, jj, h);
     if (ii < 0) H.hy[jj + 1][0] = h.hy;
     else H.hx[0][ii + 1] = h.hx;
     H.hz[jj + 1][ii + 1] = h.hz;
@@ -329,7 +336,7 @@ __device__ __forceinline__ void prefetch(Pre<R> &pf, const OpArgs<R> &a, const t
 }
 
 // y(k) at the thread's cell (gi, gj, k) from shared memory.
-template <typename R, int EPI, bool TRANSPOSE>
+template <typename R, int EPI, bool TRANSPOSE, bool RC>
 __device__ __forceinline__ void output_cell(const HTile<R> &H, const CoefTile<R> &T, const OffTile<R> &O,
                                             const OpArgs<R> &a, const Extra<R> &ex, const Pre<R> &pf,
                                             const Own<R> &own, typename CT<R>::C hxkm, typename CT<R>::C hykm,
@@ -342,9 +349,9 @@ __device__ __forceinline__ void output_cell(const HTile<R> &H, const CoefTile<R>
   const C hz00 = own.hz, hzjm = H.hz[ty][tx + 1], hzim = H.hz[ty + 1][tx];
   const C hyk = own.hy, hyim = H.hy[ty + 1][tx];
   const C hxk = own.hx, hxjm = H.hx[ty][tx + 1];
-  C yx = csub(cmul(cey, csub(hz00, hzjm)), cmul(cez, csub(hyk, hykm)));
-  C yy = csub(cmul(cez, csub(hxk, hxkm)), cmul(cex, csub(hz00, hzim)));
-  C yz = csub(cmul(cex, csub(hyk, hyim)), cmul(cey, csub(hxk, hxjm)));
+  C yx = csub(mulc<RC>(cey, csub(hz00, hzjm)), mulc<RC>(cez, csub(hyk, hykm)));
+  C yy = csub(mulc<RC>(cez, csub(hxk, hxkm)), mulc<RC>(cex, csub(hz00, hzim)));
+  C yz = csub(mulc<RC>(cex, csub(hyk, hyim)), mulc<RC>(cey, csub(hxk, hxjm)));
   const long long cell = gi + (long long)a.N[0] * (gj + (long long)a.N[1] * k);
   // pinned outputs: E_c at primal index 0 along a non-Bloch axis v ≠ c
   const bool pin_xy = !a.bloch[1] && gj == 0;
@@ -374,9 +381,15 @@ __device__ __forceinline__ void output_cell(const HTile<R> &H, const CoefTile<R>
   if (pinx) yx = czero<C>();
   if (piny) yy = czero<C>();
   if (pinz) yz = czero<C>();
-  yx = csub(yx, cmul(a.w2, dx));
-  yy = csub(yy, cmul(a.w2, dy));
-  yz = csub(yz, cmul(a.w2, dz));
+  if (a.w2.y == R(0)) {  // real ω²
+    yx = csub(yx, cscale(dx, a.w2.x));
+    yy = csub(yy, cscale(dy, a.w2.x));
+    yz = csub(yz, cscale(dz, a.w2.x));
+  } else {
+    yx = csub(yx, cmul(a.w2, dx));
+    yy = csub(yy, cmul(a.w2, dy));
+    yz = csub(yz, cmul(a.w2, dz));
+  }
   if (TRANSPOSE) {
     yx = cmul(yx, vol_e<R>(ex, 0, gi, gj, k));
     yy = cmul(yy, vol_e<R>(ex, 1, gi, gj, k));
@@ -437,6 +450,8 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2) k_apply(OpArgs<R
   const int gi = i0 + tx, gj = j0 + ty;
   const bool active = (gi < a.N[0]) && (gj < a.N[1]);
   const long long tilecol = blockIdx.x + (long long)gridDim.x * blockIdx.y;
+  // the tile's x/y coefficient tables (−1 … T) lie outside the PML
+  const bool rxy = i0 - 1 >= a.rlo[0] && i0 + TX <= a.rhi[0] && j0 - 1 >= a.rlo[1] && j0 + TY <= a.rhi[1];
   Accs<R> acc;
 
   // preamble: coefficient tables (static data, before the dependency wait);
@@ -453,7 +468,7 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2) k_apply(OpArgs<R
   typename CT<R>::C hxp, hyp;
   {
     Own<R> o;
-    curl_e<R>(S.E, S.T, a.cm[2][cidx(a, 2, k0 - 1)], (k0 + 2) % 3, k0 % 3, tx, ty, o);
+    curl_e<R, false>(S.E, S.T, a.cm[2][cidx(a, 2, k0 - 1)], (k0 + 2) % 3, k0 % 3, tx, ty, o);
     hxp = o.hx;
     hyp = o.hy;
   }
@@ -465,7 +480,9 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2) k_apply(OpArgs<R
     if (active) prefetch<R, EPI>(pf, a, aux0, gi + (long long)a.N[0] * (gj + (long long)a.N[1] * k));
     __syncthreads();  // E(k+1) present; the previous plane's reads of H are done
     Own<R> own;
-    compute_h<R>(S.E, S.H, S.T, a, k, s0, s1, tx, ty, tid, own);
+    const bool rc = rxy && k >= a.rlo[2] && k <= a.rhi[2];
+    if (rc) compute_h<R, true>(S.E, S.H, S.T, a, k, s0, s1, tx, ty, tid, own);
+    else compute_h<R, false>(S.E, S.H, S.T, a, k, s0, s1, tx, ty, tid, own);
     const bool offd = offd_on(a, tilecol, k);
     if (offd) {
       const EoffSrc<R> g{nullptr};
@@ -475,7 +492,10 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2) k_apply(OpArgs<R
     }
     zvalid = offd;
     __syncthreads();  // H(k), staged corners complete; nobody reads E(k−1) any more
-    if (active) output_cell<R, EPI, TRANSPOSE>(S.H, S.T, S.O, a, ex, pf, own, hxp, hyp, x, y, gi, gj, k, tx, ty, offd, acc);
+    if (active) {
+      if (rc) output_cell<R, EPI, TRANSPOSE, true>(S.H, S.T, S.O, a, ex, pf, own, hxp, hyp, x, y, gi, gj, k, tx, ty, offd, acc);
+      else output_cell<R, EPI, TRANSPOSE, false>(S.H, S.T, S.O, a, ex, pf, own, hxp, hyp, x, y, gi, gj, k, tx, ty, offd, acc);
+    }
     hxp = own.hx;
     hyp = own.hy;
     // E(k−1)'s slot takes E(k+2); the next iteration's first barrier orders
@@ -604,6 +624,8 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2)
   const long long tilecol = blockIdx.x + (long long)gridDim.x * blockIdx.y;
   const int kfirst = k0 - 1;  // planes kfirst … k1 are needed
   const int cx = 6 * (i0 - G::XOFF), cy = j0 - 1;
+  // the tile's x/y coefficient tables (−1 … T) lie outside the PML
+  const bool rxy = i0 - 1 >= a.rlo[0] && i0 + TX <= a.rhi[0] && j0 - 1 >= a.rlo[1] && j0 + TY <= a.rhi[1];
   Accs<R> acc;
   bool ok = true;
 
@@ -646,7 +668,7 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2)
   typename CT<R>::C hxp, hyp;
   {
     Own<R> o;
-    curl_e<R>(E, T, a.cm[2][cidx(a, 2, kfirst)], 0, 1, tx, ty, o);
+    curl_e<R, false>(E, T, a.cm[2][cidx(a, 2, kfirst)], 0, 1, tx, ty, o);
     hxp = o.hx;
     hyp = o.hy;
   }
@@ -664,7 +686,9 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2)
     }
     __syncthreads();  // E(k+1) present and fixed up; the previous plane's reads of H are done
     Own<R> own;
-    compute_h<R>(E, H, T, a, k, s0, s1, tx, ty, tid, own);
+    const bool rc = rxy && k >= a.rlo[2] && k <= a.rhi[2];
+    if (rc) compute_h<R, true>(E, H, T, a, k, s0, s1, tx, ty, tid, own);
+    else compute_h<R, false>(E, H, T, a, k, s0, s1, tx, ty, tid, own);
     const bool offd = offd_on(a, tilecol, k);
     if (offd) {
       const bool eo = G::EO_SLOT > 0 && ex.eoff_tma;
@@ -686,7 +710,10 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2)
         issue_plane<R>(smraw, bars, &tmap, &emap, a, ex, tilecol, cx, cy, i0, j0, k0, q, sm);
       }
     }
-    if (active) output_cell<R, EPI, false>(H, T, O, a, ex, pf, own, hxp, hyp, x, y, gi, gj, k, tx, ty, offd, acc);
+    if (active) {
+      if (rc) output_cell<R, EPI, false, true>(H, T, O, a, ex, pf, own, hxp, hyp, x, y, gi, gj, k, tx, ty, offd, acc);
+      else output_cell<R, EPI, false, false>(H, T, O, a, ex, pf, own, hxp, hyp, x, y, gi, gj, k, tx, ty, offd, acc);
+    }
     hxp = own.hx;
     hyp = own.hy;
   }
@@ -729,6 +756,10 @@ OpArgs<R> op_args(const fdfd_handle *h) {
   }
   a.ncell = h->ncell;
   a.oflag = h->oflag;
+  for (int w = 0; w < 3; ++w) {
+    a.rlo[w] = h->rlo[w];
+    a.rhi[w] = h->rhi[w];
+  }
   a.w2 = mk(R(h->w2[0]), R(h->w2[1]));
   return a;
 }
