@@ -1,0 +1,119 @@
+"""Full-size benchmark configurations as parity cases, through properties
+that do not depend on size.
+
+* Uneven batch (24 instances, edges 48–128, 8-cell PML, 10–60 spheres,
+  1–4 dipoles): three 48³ instances solved concurrently, one handle and one
+  host thread each; every right-hand side meets 1e-6 on the FP64 residual
+  recomputed by the GPU, and for one instance on the oracle's own assembled
+  matrix.
+* 320³ with 400 spheres (ε ∈ {1, 2.25, 12.25}): on-device smoothing, then
+  complex64 against complex128 application, the transpose identity
+  uᵀ(A v) = (Aᵀu)ᵀ v in complex128, and a capped solve whose reported
+  residual matches the FP64 residual recomputed independently.
+"""
+import threading
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+C3_48 = (1, 6, 20)   # instances of the uneven batch with 48³ grids
+
+
+def _solve_instance(pkg, q, out):
+    wl = pkg.workloads
+    mdl, om, rhs = wl.config3_instance(q)
+    A = pkg.create_A(mdl, om)
+    res = []
+    for c, p in rhs:
+        b = wl.dipole_rhs(mdl, om, c, p)
+        x, st = A.solve(b, tol=1e-6, precision="mixed")
+        res.append((b, x, st[0]))
+    # FP64 residual on the GPU, independent of the solver's own bookkeeping
+    chk = []
+    for b, x, st in res:
+        r = b - A.matvec(x)
+        chk.append(np.linalg.norm(r) / np.linalg.norm(b))
+    A.close()
+    out[q] = (mdl, om, res, chk)
+
+
+def test_uneven_batch_concurrent(pkg, oracle):
+    out = {}
+    threads = [threading.Thread(target=_solve_instance, args=(pkg, q, out)) for q in C3_48]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert sorted(out) == sorted(C3_48)
+    for q in C3_48:
+        mdl, om, res, chk = out[q]
+        assert len(res) >= 1
+        for (b, x, st), rel in zip(res, chk):
+            assert st["status"] == 0 and st["relres"] <= 1e-6, (q, st)
+            assert rel <= 1.01e-6, (q, rel)
+    # one instance against the oracle's assembled matrix
+    O = oracle
+    mdl, om, res, _ = out[C3_48[-1]]
+    g = O.uniform_grid(mdl.grid.N)
+    objs = [O.Sphere(o.shape.c, o.shape.r, o.eps) for o in mdl.objects]
+    S = O.System(g, om, mdl.Npml, objs)
+    for b, x, st in res:
+        rel = np.linalg.norm(b - S.A @ x) / np.linalg.norm(b)
+        assert rel <= 1.02e-6, rel
+
+
+@pytest.fixture(scope="module")
+def big(pkg):
+    mdl, om, rhs = pkg.workloads.config5()
+    A = pkg.create_A(mdl, om)
+    yield pkg, mdl, om, rhs, A
+    A.close()
+
+
+def test_320_smoothing_and_precisions(big):
+    import torch
+    pkg, mdl, om, rhs, A = big
+    ed, eo, sm = A.get_eps()
+    assert ed.min() >= 1.0 - 1e-12 and ed.max() <= 12.25 + 1e-12
+    assert np.count_nonzero(sm[..., :3] == 1) > 0 and np.count_nonzero(eo) > 0
+    del ed, eo, sm
+    dev = torch.device("cuda", 0)
+    g = torch.Generator(device=dev).manual_seed(5)
+    x64 = torch.randn(A.n, 2, device=dev, dtype=torch.float64, generator=g)
+    y64 = torch.empty_like(x64)
+    x32 = x64.float()
+    y32 = torch.empty_like(x32)
+    A.matvec_dev(x64.data_ptr(), y64.data_ptr(), "c128")
+    A.matvec_dev(x32.data_ptr(), y32.data_ptr(), "c64")
+    A.sync()
+    rel = (torch.linalg.vector_norm(y32.double() - y64) / torch.linalg.vector_norm(y64)).item()
+    assert rel < 1e-5, rel
+
+
+def test_320_transpose_identity(big):
+    pkg, mdl, om, rhs, A = big
+    rng = np.random.default_rng(6)
+    u = rng.standard_normal(A.n) + 1j * rng.standard_normal(A.n)
+    v = rng.standard_normal(A.n) + 1j * rng.standard_normal(A.n)
+    lhs = np.dot(u, A.matvec(v))
+    rhs_ = np.dot(A.rmatvec_transpose(u), v)
+    assert abs(lhs - rhs_) <= 1e-10 * abs(lhs), (lhs, rhs_)
+
+
+def test_320_capped_solve_residual(big):
+    import torch
+    pkg, mdl, om, rhs, A = big
+    c, p = rhs[0]
+    b = pkg.workloads.dipole_rhs(mdl, om, c, p)
+    dev = torch.device("cuda", 0)
+    bd = torch.from_numpy(b.view(np.float64).reshape(-1, 2)).to(dev)
+    xd = torch.zeros_like(bd)
+    with pytest.raises(pkg.FDFDError) as ei:
+        A.solve_dev(bd.data_ptr(), xd.data_ptr(), tol=1e-6, precision="mixed", maxit=400)
+    assert ei.value.code == 5  # not converged within the cap
+    r = torch.empty_like(bd)
+    rr = A.residual_dev(xd.data_ptr(), bd.data_ptr(), r.data_ptr())
+    rel = rr ** 0.5 / np.linalg.norm(b)
+    assert 0 < rel < 1.0
