@@ -57,6 +57,16 @@ enum { FDFD_BICGSTAB = 0, FDFD_COCG = 1 };
 
 typedef struct fdfd_handle fdfd_handle;
 
+/* 2D models (ModelTE, src/model/te.jl: E = (Ex, Ey), H = Hz; ModelTM,
+ * src/model/tm.jl: E = Ez, H = (Hx, Hy)) run as the z-invariant slice of the
+ * 3D operator: N[2] = 1, isbloch[2] = 1, e_ikl[2] = 1, where ∂z vanishes and
+ * the operator splits exactly into the TE and TM blocks.  Host field
+ * vectors then carry only the slice's components, component fastest
+ * (TE: E 2·Ncell and H Ncell complex values; TM: E Ncell and H 2·Ncell) —
+ * the reference's 2D DOF order.  Device-buffer entry points and the ε
+ * arrays keep the 3-component layout. */
+enum { FDFD_SLICE_NONE = 0, FDFD_SLICE_TE = 1, FDFD_SLICE_TM = 2 };
+
 /* Model description.  Replaces the inputs the reference feeds to
  * create_curls / create_paramops (model.jl:154-188): grid size, boundary,
  * Bloch phase, ω and the stretched ∆l arrays. */
@@ -66,7 +76,7 @@ typedef struct {
   int32_t boundft[3];       /* FDFD_EE on every axis in this build                     */
   int32_t order_cmpfirst;   /* must be 1                                               */
   int32_t device;           /* CUDA device ordinal                                     */
-  int32_t reserved;
+  int32_t slice2d;          /* FDFD_SLICE_NONE (3D), FDFD_SLICE_TE or FDFD_SLICE_TM      */
   double omega[2];          /* ω (re, im)                                              */
   double e_ikl[3][2];       /* e^{-i kbloch L} per axis (used on Bloch axes)           */
   const double *sdl_e[3];   /* s∆lₑ: N[w] complex values at E-voxel-corner planes      */
@@ -75,12 +85,13 @@ typedef struct {
 
 /* Shapes for the on-device assignment + subpixel smoothing of ε
  * (replaces add_obj! + calc_matparams!, model.jl:120-133, full.jl:16-70). */
-enum { FDFD_SHAPE_SPHERE = 0, FDFD_SHAPE_BOX = 1 };
+enum { FDFD_SHAPE_SPHERE = 0, FDFD_SHAPE_BOX = 1, FDFD_SHAPE_CYLZ = 2 };
 typedef struct {
   int32_t kind;     /* FDFD_SHAPE_*                                  */
   int32_t pad;
   double eps;       /* isotropic real ε of the object's material    */
-  double p[6];      /* sphere: cx, cy, cz, r; box: lox, loy, loz, hix, hiy, hiz */
+  double p[6];      /* sphere: cx, cy, cz, r; box: lox, loy, loz, hix, hiy, hiz;
+                       cylz (infinite along z, the 2D disk): cx, cy, r        */
 } fdfd_object;
 
 /* Optional per-cell ε design region over cells [lo, hi) (inverse design). */

@@ -9,9 +9,10 @@ reference's model/source API plus a ctypes binding of that ABI.
 from . import _lib
 from ._lib import FDFDError, load
 from .grid import DUAL, PRIM, Grid, PMLParam, create_stretched_dl, uniform_grid
-from .model import (EE, HH, Box, DesignRegion, ModelFull, Sphere, add_obj, add_srce, clear_objs, clear_srcs,
-                    create_A, create_b, create_linsys, create_stretched_dls, field_arr2vec, set_boundft, set_design,
-                    set_kbloch, set_Npml, set_ωpml, vec2field_arr)
+from .model import (EE, HH, Box, DesignRegion, Disk, ModelFull, ModelTE, ModelTM, Rect, Sphere, add_obj, add_srce,
+                    clear_objs, clear_srcs, create_A, create_b, create_linsys, create_stretched_dls, field_arr2vec,
+                    field_arr2vec_2d, set_boundft, set_design, set_kbloch, set_Npml, set_ωpml, uniform_lprim2d,
+                    vec2field_arr, vec2field_arr_2d)
 from .operator import FDFDOperator
 from . import workloads
 from .sources import PlaneSrc, PointSrc, distweights
@@ -21,4 +22,5 @@ __all__ = [
     "ModelFull", "Sphere", "Box", "DesignRegion", "add_obj", "add_srce", "clear_objs", "clear_srcs", "create_A",
     "create_b", "create_linsys", "create_stretched_dls", "set_boundft", "set_design", "set_kbloch", "set_Npml",
     "set_ωpml", "field_arr2vec", "vec2field_arr", "FDFDOperator", "PlaneSrc", "PointSrc", "distweights",
+    "ModelTE", "ModelTM", "Disk", "Rect", "uniform_lprim2d", "field_arr2vec_2d", "vec2field_arr_2d",
 ]

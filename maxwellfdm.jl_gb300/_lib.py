@@ -25,14 +25,15 @@ FDFD_C128, FDFD_C64 = 0, 1
 FDFD_EE, FDFD_HH = 0, 1
 FDFD_PREC_FP64, FDFD_PREC_MIXED = 0, 1
 FDFD_BICGSTAB, FDFD_COCG = 0, 1
-FDFD_SHAPE_SPHERE, FDFD_SHAPE_BOX = 0, 1
+FDFD_SHAPE_SPHERE, FDFD_SHAPE_BOX, FDFD_SHAPE_CYLZ = 0, 1, 2
+FDFD_SLICE_NONE, FDFD_SLICE_TE, FDFD_SLICE_TM = 0, 1, 2
 
 _dp = C.POINTER(C.c_double)
 
 
 class fdfd_desc(C.Structure):
     _fields_ = [("N", C.c_int32 * 3), ("isbloch", C.c_int32 * 3), ("boundft", C.c_int32 * 3),
-                ("order_cmpfirst", C.c_int32), ("device", C.c_int32), ("reserved", C.c_int32),
+                ("order_cmpfirst", C.c_int32), ("device", C.c_int32), ("slice2d", C.c_int32),
                 ("omega", C.c_double * 2), ("e_ikl", (C.c_double * 2) * 3),
                 ("sdl_e", _dp * 3), ("sdl_m", _dp * 3)]
 

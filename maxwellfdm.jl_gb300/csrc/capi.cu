@@ -259,8 +259,8 @@ static int matvec_host(fdfd_handle *h, const double *x, double *y, int precision
   int rc = ensure_scratch(h, precision == FDFD_C64);
   if (rc) return rc;
   const long long n = 3 * h->ncell;
-  rc = cuda_check(h, cudaMemcpyAsync(h->vx64, x, n * sizeof(double2), cudaMemcpyHostToDevice, h->stream), "H2D x");
-  if (rc) return rc;
+  const int mask = field_mask(h, false);
+  if ((rc = h2d_field(h, x, h->vx64, mask))) return rc;
   if (precision == FDFD_C64) {
     if ((rc = demote(h, h->vx32, h->vx64, n))) return rc;
     if ((rc = launch_apply_fin<float>(h, h->vx32, h->vy32, EPI_STORE, nullptr, FIN_NONE, nullptr, tr))) return rc;
@@ -268,8 +268,7 @@ static int matvec_host(fdfd_handle *h, const double *x, double *y, int precision
   } else {
     if ((rc = launch_apply_fin<double>(h, h->vx64, h->vy64, EPI_STORE, nullptr, FIN_NONE, nullptr, tr))) return rc;
   }
-  rc = cuda_check(h, cudaMemcpyAsync(y, h->vy64, n * sizeof(double2), cudaMemcpyDeviceToHost, h->stream), "D2H y");
-  if (rc) return rc;
+  if ((rc = d2h_field(h, h->vy64, y, mask))) return rc;
   rc = cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
   if (rc) return rc;
   return check_dev_err(h);
@@ -313,6 +312,11 @@ int fdfd_create(const fdfd_desc *d, fdfd_handle **out) {
     if (!d->isbloch[w] && d->N[w] < 2) return set_error(nullptr, FDFD_ERR_ARG, "N must be >= 2 on a symmetry axis");
   }
   if (d->order_cmpfirst != 1) return set_error(nullptr, FDFD_ERR_UNSUPPORTED, "order_cmpfirst = false");
+  if (d->slice2d != FDFD_SLICE_NONE) {
+    if (d->slice2d != FDFD_SLICE_TE && d->slice2d != FDFD_SLICE_TM) return set_error(nullptr, FDFD_ERR_ARG, "bad slice2d");
+    if (d->N[2] != 1 || d->isbloch[2] != 1 || d->e_ikl[2][0] != 1.0 || d->e_ikl[2][1] != 0.0)
+      return set_error(nullptr, FDFD_ERR_ARG, "a 2D slice needs N[2] = 1, isbloch[2] = 1 and e_ikl[2] = 1");
+  }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
     cudaGetLastError();
@@ -332,6 +336,7 @@ int fdfd_create(const fdfd_desc *d, fdfd_handle **out) {
   for (int w = 0; w < 3; ++w) {
     h->N[w] = d->N[w];
     h->bloch[w] = d->isbloch[w];
+    h->slice2d = d->slice2d;
     h->e_ikl[w][0] = d->e_ikl[w][0];
     h->e_ikl[w][1] = d->e_ikl[w][1];
     if (!h->bloch[w]) { h->e_ikl[w][0] = 1.0; h->e_ikl[w][1] = 0.0; }
@@ -446,6 +451,7 @@ void fdfd_destroy(fdfd_handle *h) {
   cudaFree(h->vx64);
   cudaFree(h->vy64);
   cudaFree(h->ve64);
+  cudaFree(h->stage64);
   cudaFree(h->vx32);
   cudaFree(h->vy32);
   cudaFree(h->red.part);
@@ -615,27 +621,22 @@ int fdfd_solve(fdfd_handle *h, const double *b, double *x, int32_t nrhs, const f
   if (rc) return rc;
   cudaSetDevice(h->dev);
   if ((rc = ensure_scratch(h, false))) return rc;
-  const long long n = 3 * h->ncell;
+  const int mask = field_mask(h, false);
+  const long long n = __builtin_popcount(mask) * h->ncell;  // complex entries per host vector
   int first_err = FDFD_OK;
   std::string first_msg;
   for (int q = 0; q < nrhs; ++q) {
     const double *bq = b + 2 * n * q;
     double *xq = x + 2 * n * q;
-    rc = cuda_check(h, cudaMemcpyAsync(h->vx64, bq, n * sizeof(double2), cudaMemcpyHostToDevice, h->stream), "H2D b");
-    if (rc) return rc;
-    if (opts->x0_given) {
-      rc = cuda_check(h, cudaMemcpyAsync(h->vy64, xq, n * sizeof(double2), cudaMemcpyHostToDevice, h->stream),
-                      "H2D x0");
-      if (rc) return rc;
-    }
+    if ((rc = h2d_field(h, bq, h->vx64, mask))) return rc;
+    if (opts->x0_given && (rc = h2d_field(h, xq, h->vy64, mask))) return rc;
     rc = solve_dev_impl(h, h->vx64, h->vy64, opts, stats ? stats + q : nullptr);
     if (rc && rc != FDFD_ERR_NOT_CONVERGED && rc != FDFD_ERR_BREAKDOWN) return rc;
     if (rc && first_err == FDFD_OK) {
       first_err = rc;
       first_msg = h->err;
     }
-    int rc2 = cuda_check(h, cudaMemcpyAsync(xq, h->vy64, n * sizeof(double2), cudaMemcpyDeviceToHost, h->stream),
-                         "D2H x");
+    int rc2 = d2h_field(h, h->vy64, xq, mask);
     if (rc2) return rc2;
     if ((rc2 = cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync"))) return rc2;
   }
@@ -671,19 +672,14 @@ int fdfd_eps_grad(fdfd_handle *h, const double *e, const double *g, double *grad
     h->ve64 = nullptr;
     return set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(adjoint scratch) failed");
   }
-  if ((rc = cuda_check(h, cudaMemcpyAsync(h->ve64, e, n * sizeof(double2), cudaMemcpyHostToDevice, h->stream),
-                       "H2D e")))
-    return rc;
-  if ((rc = cuda_check(h, cudaMemcpyAsync(h->vx64, g, n * sizeof(double2), cudaMemcpyHostToDevice, h->stream),
-                       "H2D g")))
-    return rc;
+  const int mask = field_mask(h, false);
+  if ((rc = h2d_field(h, e, h->ve64, mask))) return rc;
+  if ((rc = h2d_field(h, g, h->vx64, mask))) return rc;
   // λ → vy64; the gradient overwrites g's buffer (g is consumed by the solve)
   double *dgrad = reinterpret_cast<double *>(h->vx64);
   rc = eps_grad_dev_impl(h, h->ve64, h->vx64, h->vy64, dgrad, opts, stats);
   if (rc) return rc;
-  if ((rc = cuda_check(h, cudaMemcpyAsync(grad, dgrad, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream),
-                       "D2H grad")))
-    return rc;
+  if ((rc = d2h_real(h, dgrad, grad, mask))) return rc;
   return cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
 }
 
@@ -709,13 +705,10 @@ int fdfd_h_from_e(fdfd_handle *h, const double *e, const double *jm, double *hou
   int rc = ensure_scratch(h, false);
   if (!rc && jm) rc = ensure_ve(h);
   if (rc) return rc;
-  const size_t bytes = 3 * (size_t)h->ncell * sizeof(double2);
-  if ((rc = cuda_check(h, cudaMemcpyAsync(h->vx64, e, bytes, cudaMemcpyHostToDevice, h->stream), "H2D e"))) return rc;
-  if (jm && (rc = cuda_check(h, cudaMemcpyAsync(h->ve64, jm, bytes, cudaMemcpyHostToDevice, h->stream), "H2D jm")))
-    return rc;
+  if ((rc = h2d_field(h, e, h->vx64, field_mask(h, false)))) return rc;
+  if (jm && (rc = h2d_field(h, jm, h->ve64, field_mask(h, true)))) return rc;
   if ((rc = h_from_e_dev_impl(h, h->vx64, jm ? h->ve64 : nullptr, h->vy64))) return rc;
-  if ((rc = cuda_check(h, cudaMemcpyAsync(hout, h->vy64, bytes, cudaMemcpyDeviceToHost, h->stream), "D2H h")))
-    return rc;
+  if ((rc = d2h_field(h, h->vy64, hout, field_mask(h, true)))) return rc;
   return cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
 }
 
@@ -732,12 +725,10 @@ int fdfd_corner_mean(fdfd_handle *h, int32_t field, const double *in, double *ou
   cudaSetDevice(h->dev);
   int rc = ensure_scratch(h, false);
   if (rc) return rc;
-  const size_t bytes = 3 * (size_t)h->ncell * sizeof(double2);
-  if ((rc = cuda_check(h, cudaMemcpyAsync(h->vx64, in, bytes, cudaMemcpyHostToDevice, h->stream), "H2D field")))
-    return rc;
+  const int mask = field_mask(h, field == FDFD_HH);
+  if ((rc = h2d_field(h, in, h->vx64, mask))) return rc;
   if ((rc = corner_mean_dev_impl(h, field == FDFD_HH, h->vx64, h->vy64))) return rc;
-  if ((rc = cuda_check(h, cudaMemcpyAsync(out, h->vy64, bytes, cudaMemcpyDeviceToHost, h->stream), "D2H corners")))
-    return rc;
+  if ((rc = d2h_field(h, h->vy64, out, mask))) return rc;
   return cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
 }
 

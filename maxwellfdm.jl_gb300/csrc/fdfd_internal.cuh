@@ -122,6 +122,8 @@ struct fdfd_handle {
   // scratch for host-pointer entry points
   double2 *vx64 = nullptr, *vy64 = nullptr;
   double2 *ve64 = nullptr;  // adjoint entry point: the forward field
+  double2 *stage64 = nullptr;  // 2D slices: compact host-layout staging
+  int slice2d = 0;             // FDFD_SLICE_NONE / _TE / _TM
   float2 *vx32 = nullptr, *vy32 = nullptr;
   fdfd::RedBuf red{nullptr, nullptr};
   int red_blocks = 0;
@@ -175,6 +177,11 @@ int design_grad_dev_impl(fdfd_handle *h, const double *grad, double *out);
 // fields.cu
 int h_from_e_dev_impl(fdfd_handle *h, const double2 *e, const double2 *jm, double2 *hout);
 int corner_mean_dev_impl(fdfd_handle *h, int hfield, const double2 *in, double2 *out);
+// host vectors of a 2D slice carry only some components (fields.cu)
+int field_mask(const fdfd_handle *h, bool hfield);
+int h2d_field(fdfd_handle *h, const double *src, double2 *dst, int mask);
+int d2h_field(fdfd_handle *h, const double2 *src, double *dst, int mask);
+int d2h_real(fdfd_handle *h, const double *src, double *dst, int mask);
 int build_oflags(fdfd_handle *h);
 
 }  // namespace fdfd

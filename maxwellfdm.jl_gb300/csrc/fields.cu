@@ -92,6 +92,107 @@ __global__ void k_corner_mean(OpArgs<double> a, Extra<double> ex, int hfield, co
   }
 }
 
+// 2D slices (TE/TM): host vectors carry only the components in `mask`
+// (bit c = component c), component-fastest per cell.
+__global__ void k_unpack(const double2 *__restrict__ src, double2 *__restrict__ dst, int mask, long long ncell) {
+  const int nc = __popc(mask);
+  for (long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x; cell < ncell;
+       cell += (long long)gridDim.x * blockDim.x) {
+    int q = 0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      double2 v = make_double2(0.0, 0.0);
+      if (mask & (1 << c)) v = src[nc * cell + q++];
+      dst[3 * cell + c] = v;
+    }
+  }
+}
+
+__global__ void k_pack(const double2 *__restrict__ src, double2 *__restrict__ dst, int mask, long long ncell) {
+  const int nc = __popc(mask);
+  for (long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x; cell < ncell;
+       cell += (long long)gridDim.x * blockDim.x) {
+    int q = 0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      if (mask & (1 << c)) dst[nc * cell + q++] = src[3 * cell + c];
+  }
+}
+
+__global__ void k_pack_real(const double *__restrict__ src, double *__restrict__ dst, int mask, long long ncell) {
+  const int nc = __popc(mask);
+  for (long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x; cell < ncell;
+       cell += (long long)gridDim.x * blockDim.x) {
+    int q = 0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      if (mask & (1 << c)) dst[nc * cell + q++] = src[3 * cell + c];
+  }
+}
+
+int field_mask(const fdfd_handle *h, bool hfield) {
+  if (h->slice2d == FDFD_SLICE_TE) return hfield ? 4 : 3;
+  if (h->slice2d == FDFD_SLICE_TM) return hfield ? 3 : 4;
+  return 7;
+}
+
+static int ensure_stage(fdfd_handle *h) {
+  if (h->stage64) return FDFD_OK;
+  if (cudaMalloc(&h->stage64, 3 * (size_t)h->ncell * sizeof(double2)) != cudaSuccess) {
+    cudaGetLastError();
+    h->stage64 = nullptr;
+    return set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(2D staging) failed");
+  }
+  return FDFD_OK;
+}
+
+int h2d_field(fdfd_handle *h, const double *src, double2 *dst, int mask) {
+  const long long nc = h->ncell;
+  if (mask == 7)
+    return cuda_check(h, cudaMemcpyAsync(dst, src, 3 * nc * sizeof(double2), cudaMemcpyHostToDevice, h->stream),
+                      "H2D field");
+  int rc = ensure_stage(h);
+  if (rc) return rc;
+  const int n = __builtin_popcount(mask);
+  if ((rc = cuda_check(h, cudaMemcpyAsync(h->stage64, src, n * nc * sizeof(double2), cudaMemcpyHostToDevice, h->stream),
+                       "H2D field")))
+    return rc;
+  k_unpack<<<152 * 4, 256, 0, h->stream>>>(h->stage64, dst, mask, nc);
+  h->launches++;
+  return cuda_check(h, cudaGetLastError(), "k_unpack");
+}
+
+int d2h_field(fdfd_handle *h, const double2 *src, double *dst, int mask) {
+  const long long nc = h->ncell;
+  if (mask == 7)
+    return cuda_check(h, cudaMemcpyAsync(dst, src, 3 * nc * sizeof(double2), cudaMemcpyDeviceToHost, h->stream),
+                      "D2H field");
+  int rc = ensure_stage(h);
+  if (rc) return rc;
+  const int n = __builtin_popcount(mask);
+  k_pack<<<152 * 4, 256, 0, h->stream>>>(src, h->stage64, mask, nc);
+  h->launches++;
+  if ((rc = cuda_check(h, cudaGetLastError(), "k_pack"))) return rc;
+  return cuda_check(h, cudaMemcpyAsync(dst, h->stage64, n * nc * sizeof(double2), cudaMemcpyDeviceToHost, h->stream),
+                    "D2H field");
+}
+
+int d2h_real(fdfd_handle *h, const double *src, double *dst, int mask) {
+  const long long nc = h->ncell;
+  if (mask == 7)
+    return cuda_check(h, cudaMemcpyAsync(dst, src, 3 * nc * sizeof(double), cudaMemcpyDeviceToHost, h->stream),
+                      "D2H values");
+  int rc = ensure_stage(h);
+  if (rc) return rc;
+  const int n = __builtin_popcount(mask);
+  double *st = reinterpret_cast<double *>(h->stage64);
+  k_pack_real<<<152 * 4, 256, 0, h->stream>>>(src, st, mask, nc);
+  h->launches++;
+  if ((rc = cuda_check(h, cudaGetLastError(), "k_pack_real"))) return rc;
+  return cuda_check(h, cudaMemcpyAsync(dst, st, n * nc * sizeof(double), cudaMemcpyDeviceToHost, h->stream),
+                    "D2H values");
+}
+
 int h_from_e_dev_impl(fdfd_handle *h, const double2 *e, const double2 *jm, double2 *hout) {
   const OpArgs<double> a = op_args<double>(h);
   const Extra<double> ex = make_extra<double>(h);

@@ -49,6 +49,10 @@ __device__ __forceinline__ bool inside(const DevObj &o, double x, double y, doub
     const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
     return d2 <= __dmul_rn(o.p[3], o.p[3]);
   }
+  if (o.kind == FDFD_SHAPE_CYLZ) {
+    const double dx = __dsub_rn(x, o.p[0]), dy = __dsub_rn(y, o.p[1]);
+    return __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)) <= __dmul_rn(o.p[2], o.p[2]);
+  }
   return x >= o.p[0] && x <= o.p[3] && y >= o.p[1] && y <= o.p[4] && z >= o.p[2] && z <= o.p[5];
 }
 
@@ -143,6 +147,17 @@ __device__ void normal_point(const DevObj &o, const double xc[3], double n[3], d
     if (nr == 0.0) { n[0] = 1.0; n[1] = 0.0; n[2] = 0.0; }
     else { n[0] = v0 / nr; n[1] = v1 / nr; n[2] = v2 / nr; }
     for (int a = 0; a < 3; ++a) r0[a] = o.p[a] + o.p[3] * n[a];
+    return;
+  }
+  if (o.kind == FDFD_SHAPE_CYLZ) {
+    // radial in the xy-plane (the disk's normal); z follows the point
+    const double v0 = xc[0] - o.p[0], v1 = xc[1] - o.p[1], v2 = 0.0;
+    const double nr = sqrt((v0 * v0 + v1 * v1) + v2 * v2);
+    if (nr == 0.0) { n[0] = 1.0; n[1] = 0.0; n[2] = 0.0; }
+    else { n[0] = v0 / nr; n[1] = v1 / nr; n[2] = 0.0; }
+    r0[0] = o.p[0] + o.p[2] * n[0];
+    r0[1] = o.p[1] + o.p[2] * n[1];
+    r0[2] = xc[2];
     return;
   }
   double best = -INFINITY;
@@ -382,7 +397,7 @@ int smooth_objects_impl(fdfd_handle *h, const double *const lprim[3], const fdfd
     for (int i = 0; i < N; ++i) dual[w][i + 1] = mid[i];
   }
   for (int q = 0; q < nobj; ++q) {
-    if (objs[q].kind != FDFD_SHAPE_SPHERE && objs[q].kind != FDFD_SHAPE_BOX)
+    if (objs[q].kind != FDFD_SHAPE_SPHERE && objs[q].kind != FDFD_SHAPE_BOX && objs[q].kind != FDFD_SHAPE_CYLZ)
       return set_error(h, FDFD_ERR_ARG, "unknown shape kind");
     if (!(objs[q].eps > 0.0)) return set_error(h, FDFD_ERR_UNSUPPORTED, "object ε must be real and positive");
   }
@@ -455,7 +470,11 @@ int smooth_objects_impl(fdfd_handle *h, const double *const lprim[3], const fdfd
         double a[3], b[3];
         if (objs[q].kind == FDFD_SHAPE_SPHERE)
           for (int w = 0; w < 3; ++w) { a[w] = objs[q].p[w] - objs[q].p[3]; b[w] = objs[q].p[w] + objs[q].p[3]; }
-        else
+        else if (objs[q].kind == FDFD_SHAPE_CYLZ) {
+          for (int w = 0; w < 2; ++w) { a[w] = objs[q].p[w] - objs[q].p[2]; b[w] = objs[q].p[w] + objs[q].p[2]; }
+          a[2] = -HUGE_VAL;
+          b[2] = HUGE_VAL;
+        } else
           for (int w = 0; w < 3; ++w) { a[w] = objs[q].p[w]; b[w] = objs[q].p[3 + w]; }
         for (int w = 0; w < 3; ++w) {
           std::vector<double> pw(hpos[w]->begin() + ((!ext && types[w] == 1) ? 1 : 0),

@@ -19,7 +19,7 @@ struct FDFDDesc
     boundft::NTuple{3,Int32}
     order_cmpfirst::Int32
     device::Int32
-    reserved::Int32
+    slice2d::Int32
     omega::NTuple{2,Float64}
     e_ikl::NTuple{6,Float64}
     sdl_e::NTuple{3,Ptr{Float64}}

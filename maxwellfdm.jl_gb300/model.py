@@ -58,6 +58,32 @@ class Box:
         return o
 
 
+class Disk:
+    """A disk of the 2D models (the z-invariant cylinder of the slice)."""
+
+    def __init__(self, c, r):
+        self.c = np.asarray(c, dtype=np.float64)[:2]
+        self.r = float(r)
+
+    def to_c(self, eps):
+        o = _lib.fdfd_object()
+        o.kind = _lib.FDFD_SHAPE_CYLZ
+        o.eps = float(eps)
+        o.p[0], o.p[1], o.p[2] = self.c[0], self.c[1], self.r
+        return o
+
+
+class Rect:
+    """An axis-aligned rectangle of the 2D models (a box unbounded in z)."""
+
+    def __init__(self, lo, hi):
+        self.lo = np.asarray(lo, dtype=np.float64)[:2]
+        self.hi = np.asarray(hi, dtype=np.float64)[:2]
+
+    def to_c(self, eps):
+        return Box((self.lo[0], self.lo[1], -1e300), (self.hi[0], self.hi[1], 1e300)).to_c(eps)
+
+
 class _Obj:
     def __init__(self, name, shape, eps):
         self.name = name
@@ -96,11 +122,46 @@ class ModelFull:
         self.order_cmpfirst = True
 
 
+class Model2D(ModelFull):
+    """Common part of ModelTE / ModelTM: a 2D grid held as the z-invariant
+    slice of a 3D grid (one cell along z, periodic), where ∂z vanishes and
+    the 3D operator splits into the TE and TM blocks."""
+
+    slice2d = 0
+    comps = (0, 1, 2)
+
+    def __init__(self, lprim_xy, isbloch_xy=(False, False)):
+        from .grid import Grid
+        g = Grid((lprim_xy[0], lprim_xy[1], np.array([0.0, 1.0])), (isbloch_xy[0], isbloch_xy[1], True))
+        super().__init__(g)
+
+
+class ModelTE(Model2D):
+    """2D TE model: E = (Ex, Ey), H = Hz (ModelTE, src/model/te.jl:1-13)."""
+
+    slice2d = 1
+    comps = (0, 1)
+
+
+class ModelTM(Model2D):
+    """2D TM model: E = Ez, H = (Hx, Hy) (ModelTM, src/model/tm.jl)."""
+
+    slice2d = 2
+    comps = (2,)
+
+
+def uniform_lprim2d(N, h=1.0):
+    """Primal plane locations of a uniform 2D grid with N = (Nx, Ny) cells."""
+    return tuple(np.arange(N[a] + 1, dtype=np.float64) * h for a in range(2))
+
+
 def set_ωpml(mdl, ωpml):
     mdl.ωpml = ωpml
 
 
 def set_Npml(mdl, Npml):
+    if isinstance(mdl, Model2D) and len(Npml[0]) == 2:
+        Npml = (tuple(Npml[0]) + (0,), tuple(Npml[1]) + (0,))
     mdl.Npml = (tuple(int(v) for v in Npml[0]), tuple(int(v) for v in Npml[1]))
 
 
@@ -161,15 +222,29 @@ def create_A(mdl, ω, device=0):
     """The GPU operator A = Cₘ Cₑ − ω² Pε (create_A, model.jl:238-259),
     with ε assigned and smoothed on the device."""
     sdl_e, sdl_m = create_stretched_dls(mdl)
-    A = FDFDOperator(mdl.grid.N, ω, sdl_e, sdl_m, mdl.grid.isbloch, e_ikl(mdl), device)
+    A = FDFDOperator(mdl.grid.N, ω, sdl_e, sdl_m, mdl.grid.isbloch, e_ikl(mdl), device,
+                     getattr(mdl, "slice2d", 0))
     if mdl.objects or mdl.design is not None or mdl.eps_bg != 1.0:
         A.smooth_objects(mdl.grid.lprim, mdl.objects, mdl.eps_bg, mdl.design)
     return A
 
 
 def create_b(mdl, ω):
-    """b = −iω jₑ (create_b, model.jl:264-287, jₘ = 0)."""
+    """b = −iω jₑ (create_b, model.jl:264-287, jₘ = 0); for a 2D model, the
+    slice's components only (component fastest)."""
+    if isinstance(mdl, Model2D):
+        return -1j * ω * field_arr2vec_2d(mdl.je[:, :, 0, list(mdl.comps)])
     return -1j * ω * field_arr2vec(mdl.je)
+
+
+def field_arr2vec_2d(F):
+    """(Nx,Ny,m) → component-fastest vector of a 2D model."""
+    F = np.asarray(F)
+    return np.ascontiguousarray(np.transpose(F, (1, 0, 2))).reshape(-1)
+
+
+def vec2field_arr_2d(v, N, m):
+    return np.transpose(np.asarray(v).reshape(N[1], N[0], m), (1, 0, 2))
 
 
 def create_linsys(mdl, ω, device=0):

@@ -17,11 +17,17 @@ from ._lib import check, dptr
 class FDFDOperator:
     """Matrix-free A on the GPU (complex128 semantics, DOF order c + 3·cell)."""
 
-    def __init__(self, N, omega, sdl_e, sdl_m, isbloch=(False, False, False), e_ikl=(1, 1, 1), device=0):
+    def __init__(self, N, omega, sdl_e, sdl_m, isbloch=(False, False, False), e_ikl=(1, 1, 1), device=0,
+                 slice2d=0):
+        """slice2d: 0 (3D), 1 (TE) or 2 (TM) — a 2D model as the z-invariant
+        slice (N[2] = 1, Bloch z); host field vectors then carry only the
+        slice's components (TE: E = (Ex, Ey), H = Hz; TM: E = Ez, H = (Hx, Hy))."""
         lib = _lib.load()
         self.N = tuple(int(n) for n in N)
         self.ncell = self.N[0] * self.N[1] * self.N[2]
-        self.n = 3 * self.ncell
+        self.slice2d = int(slice2d)
+        self.ncomp_e, self.ncomp_h = {0: (3, 3), 1: (2, 1), 2: (1, 2)}[self.slice2d]
+        self.n = self.ncomp_e * self.ncell
         self.omega = complex(omega)
         d = _lib.fdfd_desc()
         self._keep = []
@@ -40,6 +46,7 @@ class FDFDOperator:
             d.sdl_m[w] = dptr(sm)
         d.order_cmpfirst = 1
         d.device = int(device)
+        d.slice2d = self.slice2d
         d.omega[0], d.omega[1] = self.omega.real, self.omega.imag
         h = C.c_void_p()
         check(lib.fdfd_create(C.byref(d), C.byref(h)))
@@ -115,8 +122,8 @@ class FDFDOperator:
 
     def get_eps(self):
         """Returns (eps_diag, eps_off, smask) as (Nx,Ny,Nz,3|4) arrays."""
-        ed = np.zeros(self.n)
-        eo = np.zeros(self.n)
+        ed = np.zeros(3 * self.ncell)    # ε keeps the 3-component layout in every mode
+        eo = np.zeros(3 * self.ncell)
         sm = np.zeros(4 * self.ncell, dtype=np.uint8)
         self._check(self._lib.fdfd_get_eps(self._h, dptr(ed), dptr(eo), sm.ctypes.data_as(C.POINTER(C.c_uint8))))
         return (_aos_cell(ed, self.N, 3), _aos_cell(eo, self.N, 3), _aos_cell(sm, self.N, 4))
@@ -132,6 +139,8 @@ class FDFDOperator:
 
     def rmatvec_transpose(self, x, precision="c128"):
         x = np.ascontiguousarray(x, dtype=np.complex128).reshape(-1)
+        if x.size != self.n:
+            raise ValueError("x has the wrong length")
         y = np.empty_like(x)
         self._check(self._lib.fdfd_matvec_transpose(self._h, dptr(x), dptr(y), _prec(precision)))
         return y
@@ -193,7 +202,9 @@ class FDFDOperator:
         if e.size != self.n:
             raise ValueError("e has the wrong length")
         jmv = None if jm is None else np.ascontiguousarray(jm, dtype=np.complex128).reshape(-1)
-        out = np.empty_like(e)
+        if jmv is not None and jmv.size != self.ncomp_h * self.ncell:
+            raise ValueError("jm has the wrong length")
+        out = np.empty(self.ncomp_h * self.ncell, dtype=np.complex128)
         self._check(self._lib.fdfd_h_from_e(self._h, dptr(e), None if jmv is None else dptr(jmv), dptr(out)))
         return out
 
@@ -201,7 +212,7 @@ class FDFDOperator:
         """create_Mcs corner interpolation (model.jl:287-306): field "E" → Mcₑ v
         (primal corners), "H" → Mcₘ v (dual corners)."""
         v = np.ascontiguousarray(v, dtype=np.complex128).reshape(-1)
-        if v.size != self.n:
+        if v.size != (self.ncomp_e if field == "E" else self.ncomp_h) * self.ncell:
             raise ValueError("field vector has the wrong length")
         f = {"E": _lib.FDFD_EE, "H": _lib.FDFD_HH}[field]
         out = np.empty_like(v)
@@ -221,13 +232,15 @@ class FDFDOperator:
         o = self._opts(tol, precision, "bicgstab", maxit, False, delta, check_every, True, use_graph)
         st = _lib.fdfd_stats()
         self._check(self._lib.fdfd_eps_grad(self._h, dptr(e), dptr(g), dptr(grad), C.byref(o), C.byref(st)))
-        return _aos_cell(grad, self.N, 3), st.as_dict()
+        return _aos_cell(grad, self.N, self.ncomp_e), st.as_dict()
 
     def design_grad(self, grad):
         """Chain dL/dε_ww ((Nx,Ny,Nz,3), as eps_grad returns it) to the cells
         of the design region applied by smooth_objects → (hi−lo) array."""
         if self._design_shape is None:
             raise ValueError("no design region was applied")
+        if self.slice2d:
+            raise ValueError("design regions are 3D only")
         gv = _cell_aos(grad, self.N, np.float64)
         ds = self._design_shape
         out = np.empty(ds[0] * ds[1] * ds[2])

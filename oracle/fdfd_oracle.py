@@ -609,6 +609,32 @@ class Sphere:
         return n, self.c + self.r * n
 
 
+class CylinderZ:
+    """A disk of the 2D models: the cylinder x²+y² ≤ r² unbounded in z (the
+    z-invariant slice of a 2D shape).  Normal radial in the xy-plane."""
+    kind = "cylz"
+
+    def __init__(self, c, r, eps):
+        self.c = np.asarray(c, dtype=np.float64)[:2]
+        self.r = float(r)
+        self.eps = float(eps)
+
+    def contains(self, X, Y, Z):
+        dx = X - self.c[0]
+        dy = Y - self.c[1]
+        return dx * dx + dy * dy <= self.r * self.r
+
+    def normal_point(self, xc):
+        v0 = xc[0] - self.c[0]
+        v1 = xc[1] - self.c[1]
+        nr = math.sqrt((v0 * v0 + v1 * v1) + 0.0 * 0.0)
+        if nr == 0.0:
+            n = np.array([1.0, 0.0, 0.0])
+        else:
+            n = np.array([v0 / nr, v1 / nr, 0.0])
+        return n, np.array([self.c[0] + self.r * n[0], self.c[1] + self.r * n[1], xc[2]])
+
+
 class Box:
     kind = "box"
 
