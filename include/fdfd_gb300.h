@@ -154,6 +154,14 @@ int fdfd_smooth_objects(fdfd_handle *h, const double *const lprim[3],
  * 2 design).  Any pointer may be NULL. */
 int fdfd_get_eps(fdfd_handle *h, double *eps_diag, double *eps_off, uint8_t *smask);
 
+/* Field solved for (create_linsys's ft, model.jl:238-240, 266-268):
+ * FDFD_EE (default) — A = Cₘ Cₑ − ω² Pε on E; FDFD_HH — A = Cₑ (Pε \ Cₘ) − ω² Pμ
+ * on H (Pμ = I), for which ε must be diagonal as in the reference.  Under
+ * FDFD_HH the matvec and solve entry points take H vectors (same DOF
+ * order); transpose, COCG, the ε gradient and the allocation-free residual
+ * are E-formulation only (FDFD_ERR_UNSUPPORTED). */
+int fdfd_set_field_type(fdfd_handle *h, int32_t ft);
+
 /* ---- operator application --------------------------------------------------
  * y = A x (mul!(y, A, x) on the reference's assembled A, model.jl:238-259).
  * Host buffers: 2·3·Ncell doubles (ComplexF64).  precision = FDFD_C64

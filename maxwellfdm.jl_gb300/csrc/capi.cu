@@ -259,7 +259,7 @@ static int matvec_host(fdfd_handle *h, const double *x, double *y, int precision
   int rc = ensure_scratch(h, precision == FDFD_C64);
   if (rc) return rc;
   const long long n = 3 * h->ncell;
-  const int mask = field_mask(h, false);
+  const int mask = field_mask(h, h->ft == FDFD_HH);  // the unknown field's components
   if ((rc = h2d_field(h, x, h->vx64, mask))) return rc;
   if (precision == FDFD_C64) {
     if ((rc = demote(h, h->vx32, h->vx64, n))) return rc;
@@ -597,6 +597,8 @@ static int check_opts(fdfd_handle *h, const fdfd_solve_opts *o) {
   if (o->precision == FDFD_PREC_MIXED && !(o->delta > 0.0 && o->delta < 1.0))
     return set_error(h, FDFD_ERR_ARG, "delta must be in (0, 1)");
   if (o->transpose && !transpose_ok(h)) return set_error(h, FDFD_ERR_UNSUPPORTED, "transpose with a Bloch phase");
+  if (h->ft == FDFD_HH && (o->transpose || o->method == FDFD_COCG))
+    return set_error(h, FDFD_ERR_UNSUPPORTED, "the H formulation solves the forward system with BiCGSTAB");
   if (o->method == FDFD_COCG && o->precision == FDFD_PREC_MIXED)
     return set_error(h, FDFD_ERR_UNSUPPORTED, "COCG runs in FP64 only (its complex64 recurrence does not converge)");
   if (o->method == FDFD_COCG && o->transpose)
@@ -621,7 +623,7 @@ int fdfd_solve(fdfd_handle *h, const double *b, double *x, int32_t nrhs, const f
   if (rc) return rc;
   cudaSetDevice(h->dev);
   if ((rc = ensure_scratch(h, false))) return rc;
-  const int mask = field_mask(h, false);
+  const int mask = field_mask(h, h->ft == FDFD_HH);  // the unknown field's components
   const long long n = __builtin_popcount(mask) * h->ncell;  // complex entries per host vector
   int first_err = FDFD_OK;
   std::string first_msg;
@@ -650,6 +652,7 @@ int fdfd_eps_grad_dev(fdfd_handle *h, const void *e, const void *g, void *lam, d
   int rc = check_opts(h, opts);
   if (rc) return rc;
   if (opts->method != FDFD_BICGSTAB) return set_error(h, FDFD_ERR_UNSUPPORTED, "the adjoint solve uses BiCGSTAB");
+  if (h->ft != FDFD_EE) return set_error(h, FDFD_ERR_UNSUPPORTED, "the ε gradient is for the E formulation");
   if (!transpose_ok(h)) return set_error(h, FDFD_ERR_UNSUPPORTED, "adjoint with a Bloch phase");
   cudaSetDevice(h->dev);
   rc = eps_grad_dev_impl(h, (const double2 *)e, (const double2 *)g, (double2 *)lam, grad, opts, stats);
@@ -663,6 +666,7 @@ int fdfd_eps_grad(fdfd_handle *h, const double *e, const double *g, double *grad
   int rc = check_opts(h, opts);
   if (rc) return rc;
   if (opts->method != FDFD_BICGSTAB) return set_error(h, FDFD_ERR_UNSUPPORTED, "the adjoint solve uses BiCGSTAB");
+  if (h->ft != FDFD_EE) return set_error(h, FDFD_ERR_UNSUPPORTED, "the ε gradient is for the E formulation");
   if (!transpose_ok(h)) return set_error(h, FDFD_ERR_UNSUPPORTED, "adjoint with a Bloch phase");
   cudaSetDevice(h->dev);
   if ((rc = ensure_scratch(h, false))) return rc;
@@ -730,6 +734,16 @@ int fdfd_corner_mean(fdfd_handle *h, int32_t field, const double *in, double *ou
   if ((rc = corner_mean_dev_impl(h, field == FDFD_HH, h->vx64, h->vy64))) return rc;
   if ((rc = d2h_field(h, h->vy64, out, mask))) return rc;
   return cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
+}
+
+int fdfd_set_field_type(fdfd_handle *h, int32_t ft) {
+  if (!h) return set_error(h, FDFD_ERR_ARG, "null handle");
+  if (ft != FDFD_EE && ft != FDFD_HH) return set_error(h, FDFD_ERR_ARG, "field type must be FDFD_EE or FDFD_HH");
+  if (ft == FDFD_HH && h->has_off)
+    return set_error(h, FDFD_ERR_UNSUPPORTED, "the H formulation needs a diagonal ε (Pε \\ Cₘ)");
+  h->ft = ft;
+  fdfd::drop_graphs(h);
+  return FDFD_OK;
 }
 
 int fdfd_design_grad_dev(fdfd_handle *h, const double *grad, double *dgrad) {

@@ -124,6 +124,7 @@ struct fdfd_handle {
   double2 *ve64 = nullptr;  // adjoint entry point: the forward field
   double2 *stage64 = nullptr;  // 2D slices: compact host-layout staging
   int slice2d = 0;             // FDFD_SLICE_NONE / _TE / _TM
+  int ft = 0;                  // field solved for: FDFD_EE (A = CₘCₑ − ω²Pε) or FDFD_HH (A = CₑPε⁻¹Cₘ − ω²)
   float2 *vx32 = nullptr, *vy32 = nullptr;
   fdfd::RedBuf red{nullptr, nullptr};
   int red_blocks = 0;
@@ -182,6 +183,10 @@ int field_mask(const fdfd_handle *h, bool hfield);
 int h2d_field(fdfd_handle *h, const double *src, double2 *dst, int mask);
 int d2h_field(fdfd_handle *h, const double2 *src, double *dst, int mask);
 int d2h_real(fdfd_handle *h, const double *src, double *dst, int mask);
+// the H formulation's operator (hh.cu)
+template <typename R>
+int launch_apply_hh(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R>::C *y, int epi,
+                    const typename CT<R>::C *aux0, int fin, KScalars *sc);
 int build_oflags(fdfd_handle *h);
 
 }  // namespace fdfd

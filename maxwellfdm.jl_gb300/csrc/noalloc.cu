@@ -65,6 +65,7 @@ using namespace fdfd;
 
 extern "C" int fdfd_residual_dev_noalloc(fdfd_handle *h, const void *x, const void *b, void *r, double *rnorm2) {
   if (!h || !x || !b || !r || !rnorm2) return set_error(h, FDFD_ERR_ARG, "null argument");
+  if (h->ft != FDFD_EE) return set_error(h, FDFD_ERR_UNSUPPORTED, "the allocation-free residual is for the E formulation");
   int rc = cuda_check(h, cudaSetDevice(h->dev), "cudaSetDevice");
   if (rc) return rc;
   unsigned char *base = nullptr;

@@ -1021,6 +1021,10 @@ int launch_residual_ext(fdfd_handle *h, const double2 *x, double2 *r, const doub
 template <typename R>
 int launch_apply_fin(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R>::C *y, int epi,
                      const typename CT<R>::C *aux0, int fin, KScalars *sc, bool transpose) {
+  if (h->ft == FDFD_HH) {
+    if (transpose) return set_error(h, FDFD_ERR_UNSUPPORTED, "transpose of the H formulation");
+    return launch_apply_hh<R>(h, x, y, epi, aux0, fin, sc);
+  }
   if (transpose) {
     switch (epi) {
       case EPI_STORE: return launch_t<R, EPI_STORE, true>(h, x, y, aux0, fin, sc);

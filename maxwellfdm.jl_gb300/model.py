@@ -218,20 +218,35 @@ def vec2field_arr(v, N):
     return np.transpose(np.asarray(v).reshape(N[2], N[1], N[0], 3), (2, 1, 0, 3))
 
 
-def create_A(mdl, ω, device=0):
-    """The GPU operator A = Cₘ Cₑ − ω² Pε (create_A, model.jl:238-259),
-    with ε assigned and smoothed on the device."""
+def create_A(mdl, ω, device=0, ft=EE):
+    """The GPU operator (create_A, model.jl:238-259) with ε assigned and
+    smoothed on the device: ft = EE → A = Cₘ Cₑ − ω² Pε on E; ft = HH →
+    A = Cₑ (Pε \\ Cₘ) − ω² on H (diagonal ε only, as in the reference)."""
     sdl_e, sdl_m = create_stretched_dls(mdl)
     A = FDFDOperator(mdl.grid.N, ω, sdl_e, sdl_m, mdl.grid.isbloch, e_ikl(mdl), device,
                      getattr(mdl, "slice2d", 0))
     if mdl.objects or mdl.design is not None or mdl.eps_bg != 1.0:
         A.smooth_objects(mdl.grid.lprim, mdl.objects, mdl.eps_bg, mdl.design)
+    if ft == HH:
+        A.set_field_type("H")
     return A
 
 
-def create_b(mdl, ω):
+def create_b(mdl, ω, ft=EE, A=None):
     """b = −iω jₑ (create_b, model.jl:264-287, jₘ = 0); for a 2D model, the
-    slice's components only (component fastest)."""
+    slice's components only (component fastest).  ft = HH: b = Cₑ (Pε \\ jₑ),
+    formed on the GPU by the operator A of the same model (its ε and its
+    curl), as (−iω)·h_from_e(ε⁻¹ jₑ)."""
+    if ft == HH:
+        if A is None:
+            raise ValueError("the H formulation's b needs the model's operator A")
+        ed, _, _ = A.get_eps()
+        je = mdl.je / ed
+        if isinstance(mdl, Model2D):
+            x = field_arr2vec_2d(je[:, :, 0, [c for c in (0, 1, 2) if c in mdl.comps]])
+        else:
+            x = field_arr2vec(je)
+        return -1j * ω * A.h_from_e(x)
     if isinstance(mdl, Model2D):
         return -1j * ω * field_arr2vec_2d(mdl.je[:, :, 0, list(mdl.comps)])
     return -1j * ω * field_arr2vec(mdl.je)
@@ -247,5 +262,6 @@ def vec2field_arr_2d(v, N, m):
     return np.transpose(np.asarray(v).reshape(N[1], N[0], m), (1, 0, 2))
 
 
-def create_linsys(mdl, ω, device=0):
-    return create_A(mdl, ω, device), create_b(mdl, ω)
+def create_linsys(mdl, ω, device=0, ft=EE):
+    A = create_A(mdl, ω, device, ft)
+    return A, create_b(mdl, ω, ft, A)

@@ -84,6 +84,16 @@ class FDFDOperator:
 
     # ---------------------------------------------------------------- material
     _design_shape = None
+    ft = "E"
+
+    def set_field_type(self, ft):
+        """Solve for E (A = CₘCₑ − ω²Pε) or H (A = Cₑ(Pε \\ Cₘ) − ω², diagonal ε
+        only) — create_linsys's ft (model.jl:238-240)."""
+        if ft not in ("E", "H"):
+            raise ValueError("ft must be 'E' or 'H'")
+        self._check(self._lib.fdfd_set_field_type(self._h, _lib.FDFD_EE if ft == "E" else _lib.FDFD_HH))
+        self.ft = ft
+        self.n = (self.ncomp_e if ft == "E" else self.ncomp_h) * self.ncell
 
     def set_eps(self, eps_diag, eps_off=None):
         """eps_diag, eps_off: (Nx,Ny,Nz,3) real arrays (ε_cc at E_c; ε_xy, ε_yz,

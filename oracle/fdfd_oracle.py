@@ -460,6 +460,24 @@ def create_A(omega, Peps, Ce, Cm):
     return A.tocsr()
 
 
+def create_A_hh(omega, eps_diag_vec, Ce, Cm):
+    """H formulation: A = Cₑ·(Pε \\ Cₘ) − ω²·Pμ with Pμ = I and a diagonal
+    Pε (model.jl:238-240; the reference divides by Pε only when it is
+    diagonal).  eps_diag_vec: ε at every E sample (DOF order)."""
+    A = Ce @ sp.diags(1.0 / np.asarray(eps_diag_vec, dtype=np.complex128)) @ Cm
+    if omega != 0:
+        A = A - (omega ** 2) * sp.identity(Ce.shape[0], dtype=np.complex128, format="csr")
+    return A.tocsr()
+
+
+def create_b_hh(omega, eps_diag_vec, Ce, je_vec, jm_vec=None):
+    """b = Cₑ (Pε \\ jₑ) − iω jₘ (model.jl:266-268)."""
+    b = Ce @ (np.asarray(je_vec, dtype=np.complex128) / np.asarray(eps_diag_vec, dtype=np.complex128))
+    if jm_vec is not None and omega != 0:
+        b = b - (1j * omega) * jm_vec
+    return b
+
+
 def create_b(omega, je_vec, jm_vec=None, Cm=None):
     """b = -Cₘ(Pμ⁻¹ jₘ) - iω jₑ (model.jl:275-278)."""
     b = np.zeros_like(je_vec, dtype=np.complex128)
