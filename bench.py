@@ -4,12 +4,12 @@ dielectric-sphere scatterer (40 spheres, ε = 12.25, 10-cell PML, λ = 16,
 x-polarised current sheet at z = 15), mixed precision versus FP64 on the same
 GB300, plus the HBM roofline of the operator kernel.
 
-A step is one complete mixed-precision BiCGSTAB solve (complex64 operator and
+A step is one complete mixed-precision BiCGStab(4) solve (complex64 operator and
 Krylov vectors, FP64 reductions and reliable FP64 residual replacement) with
 b resident in HBM.  The same workload is also solved once in plain complex128
 (the FP64 comparison), end to end through the C ABI with host buffers
-(``e2e``), and — on a bounded sample — by an OpenMP complex128 CSR BiCGSTAB
-of the assembled A on all host cores (``cpu_baseline``).
+(``e2e``), and — on a bounded sample — by an OpenMP complex128 CSR BiCGStab(4)
+of the assembled A on all host cores (``cpu_baseline``), the same algorithm.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -34,6 +34,7 @@ METRIC = "time to 1e-6 rel. residual, mixed vs FP64 on same GB300; matvec HBM GB
 WORKLOAD = "96^3 dielectric-sphere scatterer: 40 spheres r~U[3,8] eps=12.25, 10-cell PML, lambda=16, x-pol sheet z=15"
 PROFILE_NOTE = os.path.join(ROOT, "profiles", "solve_96cube_spheres.md")
 NCU_NOTE = os.path.join(ROOT, "profiles", "stencil_c64_96cube.md")
+METHOD, ELL = "bicgstabl", 4   # BiCGStab(4) in both precisions
 
 
 def _dist():
@@ -117,13 +118,14 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def _recorded_fp64_iterations():
-    """FP64 BiCGSTAB iteration count for this workload, recorded from a GPU
-    run in profiles/ (the CPU sparse BiCGSTAB runs the same recurrence)."""
+def _recorded_fp64_matvecs():
+    """Operator applications of the FP64 BiCGStab(4) solve of this workload,
+    recorded from a GPU run in profiles/ (the CPU baseline runs the same
+    recurrence, so it needs the same count)."""
     try:
         with open(PROFILE_NOTE) as f:
             for line in f:
-                if line.startswith("fp64_bicgstab_iterations:"):
+                if line.startswith("fp64_bicgstabl_matvecs:"):
                     return int(line.split(":")[1])
     except OSError:
         pass
@@ -146,7 +148,7 @@ _CPU = {}
 
 def _cpu_system():
     """The oracle's assembled complex128 CSR A and b for this workload (built
-    once), held for the OpenMP CSR BiCGSTAB of oracle/csr_bicgstab.c on all
+    once), held for the OpenMP CSR BiCGStab(4) of oracle/csr_bicgstab.c on all
     host cores."""
     if not _CPU:
         import __graft_entry__ as ge
@@ -168,27 +170,27 @@ def _cpu_system():
 
 
 def cpu_sample(seconds=8.0):
-    """Time per FP64 BiCGSTAB iteration of the CPU baseline over a bounded
-    sample (about `seconds` of work, at least 10 iterations)."""
+    """Time per operator application of the CPU baseline's FP64 BiCGStab(4)
+    over a bounded sample (about `seconds` of work, at least 3 cycles)."""
     c = _cpu_system()
     M, b = c["M"], c["b"]
     t0 = time.perf_counter()
-    M.bicgstab(b, tol=1e-300, maxit=4)
-    t_est = (time.perf_counter() - t0) / 4
-    iters = int(min(5000, max(10, seconds / max(t_est, 1e-6))))
+    _, mv, _ = M.bicgstabl(b, ell=4, tol=1e-300, maxmv=8)
+    t_est = (time.perf_counter() - t0) / max(mv, 1)
+    mvs = int(min(20000, max(24, seconds / max(t_est, 1e-6))))
     t0 = time.perf_counter()
-    _, it, _ = M.bicgstab(b, tol=1e-300, maxit=iters)
-    t_it = (time.perf_counter() - t0) / max(it, 1)
-    return {"t_iter": t_it, "iters": it, "t_assemble": c["t_asm"], "nnz": M.nnz, "threads": M.threads}
+    _, mv, _ = M.bicgstabl(b, ell=4, tol=1e-300, maxmv=mvs)
+    t_mv = (time.perf_counter() - t0) / max(mv, 1)
+    return {"t_mv": t_mv, "matvecs": mv, "t_assemble": c["t_asm"], "nnz": M.nnz, "threads": M.threads}
 
 
 def run_reference(args):
     ws, rank, local = _dist()
     if rank != 0:
         return 0
-    n_iter = _recorded_fp64_iterations()
-    if n_iter is None:
-        print(json.dumps({"impl": "reference", "unavailable": "no recorded FP64 iteration count to project the "
+    n_mv = _recorded_fp64_matvecs()
+    if n_mv is None:
+        print(json.dumps({"impl": "reference", "unavailable": "no recorded FP64 operator count to project the "
                                                               "CPU sample onto (profiles/ note missing)"}))
         return 0
     samples = []
@@ -196,17 +198,17 @@ def run_reference(args):
     for s in range(args.warmup + args.steps):
         r = cpu_sample(seconds=6.0)
         if s >= args.warmup:
-            samples.append(r["t_iter"])
-    t_iter = statistics.median(samples)
-    value = t_iter * n_iter
-    sample = (f"{args.steps} samples of {r['iters']} FP64 BiCGSTAB iterations (complex128 CSR, {r['nnz']} nnz, "
-              f"OpenMP on {r['threads']} host threads, oracle/csr_bicgstab.c) on the same 96^3 system; median "
-              f"{t_iter*1e3:.2f} ms/iteration projected to {n_iter} iterations (the FP64 BiCGSTAB count to 1e-6 "
-              f"for this system)")
+            samples.append(r["t_mv"])
+    t_mv = statistics.median(samples)
+    value = t_mv * n_mv
+    sample = (f"{args.steps} samples of {r['matvecs']} operator applications of FP64 BiCGStab(4) (complex128 CSR, "
+              f"{r['nnz']} nnz, OpenMP on {r['threads']} host threads, oracle/csr_bicgstab.c) on the same 96^3 "
+              f"system; median {t_mv*1e3:.2f} ms per application projected to {n_mv} applications (the FP64 "
+              f"BiCGStab(4) count to 1e-6 for this system)")
     line = {"metric": METRIC, "value": value, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": t_iter * r["iters"] * 1e3, "higher_is_better": False,
+            "warmup": args.warmup, "ms_per_step": t_mv * r["matvecs"] * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded)", "impl": "reference",
-            "config": {"workload": WORKLOAD, "precision": "fp64", "solver": "BiCGSTAB"},
+            "config": {"workload": WORKLOAD, "precision": "fp64", "solver": "BiCGStab(4)"},
             "cpu_baseline": {"value": value, "unit": "s", "cores": r["threads"], "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -232,7 +234,7 @@ def run_ours(args):
     x_dev = torch.zeros_like(b_dev)
     tol = 1e-6
     for _ in range(args.warmup):
-        A.solve_dev(b_dev.data_ptr(), x_dev.data_ptr(), tol=tol, precision="mixed")
+        A.solve_dev(b_dev.data_ptr(), x_dev.data_ptr(), tol=tol, precision="mixed", method=METHOD, ell=ELL)
     torch.cuda.synchronize(dev)
     _barrier(ws)
     clk = ClockSampler(local)
@@ -243,7 +245,7 @@ def run_ours(args):
     torch.cuda.synchronize(dev)
     for _ in range(args.steps):
         ev0.record(stream)
-        st = A.solve_dev(b_dev.data_ptr(), x_dev.data_ptr(), tol=tol, precision="mixed")
+        st = A.solve_dev(b_dev.data_ptr(), x_dev.data_ptr(), tol=tol, precision="mixed", method=METHOD, ell=ELL)
         ev1.record(stream)
         ev1.synchronize()
         times.append(ev0.elapsed_time(ev1) / 1e3)
@@ -257,7 +259,8 @@ def run_ours(args):
     # FP64 comparison on the same GPU (one solve)
     x64_dev = torch.zeros_like(b_dev)
     ev0.record(stream)
-    st64 = A.solve_dev(b_dev.data_ptr(), x64_dev.data_ptr(), tol=tol, precision="fp64")
+    st64 = A.solve_dev(b_dev.data_ptr(), x64_dev.data_ptr(), tol=tol, precision="fp64", method=METHOD,
+                       ell=ELL)
     ev1.record(stream)
     ev1.synchronize()
     t_fp64 = max_over_ranks(ev0.elapsed_time(ev1) / 1e3, ws, dev)
@@ -308,7 +311,8 @@ def run_ours(args):
     e2e_t = []
     for _ in range(max(1, args.steps)):
         t0 = time.perf_counter()
-        xs, _st = A.solve(bh.numpy().view(np.complex128).reshape(-1), tol=tol, precision="mixed")
+        xs, _st = A.solve(bh.numpy().view(np.complex128).reshape(-1), tol=tol, precision="mixed", method=METHOD,
+                         ell=ELL)
         e2e_t.append(time.perf_counter() - t0)
     e2e = max_over_ranks(statistics.mean(e2e_t), ws, dev)
 
@@ -317,23 +321,24 @@ def run_ours(args):
         cpu = None
         if not args.no_cpu:
             r = cpu_sample(seconds=10.0)
-            proj = r["t_iter"] * st64["iterations"]
+            proj = r["t_mv"] * st64["matvecs"]
             cpu = {"value": proj, "unit": "s", "cores": r["threads"], "kind": "port",
-                   "sample": (f"{r['iters']} FP64 BiCGSTAB iterations of the CPU baseline (complex128 CSR, "
-                              f"{r['nnz']} nnz, OpenMP on {r['threads']} host threads) on the same system: "
-                              f"{r['t_iter']*1e3:.2f} ms/iteration, projected to the {st64['iterations']} FP64 "
-                              f"iterations this run needed")}
+                   "sample": (f"{r['matvecs']} operator applications of FP64 BiCGStab(4) on the CPU baseline "
+                              f"(complex128 CSR, {r['nnz']} nnz, OpenMP on {r['threads']} host threads) on the same "
+                              f"system: {r['t_mv']*1e3:.2f} ms per application, projected to the {st64['matvecs']} "
+                              f"applications the FP64 GPU solve needed")}
         line = {
             "metric": METRIC, "value": t_mixed, "unit": "s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_mixed * 1e3, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "c64 (FP64 reductions and residual replacement)",
             "data": "synthetic (seeded spheres, seed 1000+rank)",
-            "config": {"workload": WORKLOAD, "cells": A.ncell, "unknowns": n, "solver": "BiCGSTAB",
+            "config": {"workload": WORKLOAD, "cells": A.ncell, "unknowns": n, "solver": "BiCGStab(4)",
                        "tol": tol, "l2": "solve working set > L2 (8 c64 + 3 c128 vectors = 0.5 GB); L2 flushed "
                                          "by a 256 MiB read before each roofline launch",
                        "parallelism": "replicas" if ws > 1 else "1 GPU"},
             "fp64_time_s": t_fp64, "mixed_speedup_vs_fp64": t_fp64 / t_mixed,
             "iterations": stats[-1]["iterations"], "fp64_iterations": st64["iterations"],
+            "matvecs": stats[-1]["matvecs"], "fp64_matvecs": st64["matvecs"],
             "refinements": stats[-1]["refinements"], "relres": stats[-1]["relres"],
             "fp64_relres": st64["relres"], "field_err_vs_fp64": ferr,
             "matvec_c64_us": t_mv * 1e6, "matvec_c128_us": t_mv128 * 1e6,

@@ -52,8 +52,9 @@ enum { FDFD_C128 = 0, FDFD_C64 = 1 };
 enum { FDFD_EE = 0, FDFD_HH = 1 };
 /* solver precision */
 enum { FDFD_PREC_FP64 = 0, FDFD_PREC_MIXED = 1 };
-/* Krylov method */
-enum { FDFD_BICGSTAB = 0, FDFD_COCG = 1 };
+/* Krylov method: BiCGSTAB; Jacobi-preconditioned COCG on the symmetrised
+ * operator (FP64 only); BiCGStab(ℓ) (Sleijpen–Fokkema), ℓ = opts.ell ≤ 4 */
+enum { FDFD_BICGSTAB = 0, FDFD_COCG = 1, FDFD_BICGSTABL = 2 };
 
 typedef struct fdfd_handle fdfd_handle;
 
@@ -111,6 +112,7 @@ typedef struct {
   int32_t check_every;      /* iterations per launched batch between host checks       */
   int32_t transpose;        /* 1: solve Aᵀ x = b (adjoint)                             */
   int32_t use_graph;        /* 1: replay each batch as a CUDA graph                     */
+  int32_t ell;              /* FDFD_BICGSTABL: degree ℓ of the minimal-residual part (1–4) */
 } fdfd_solve_opts;
 
 typedef struct {
@@ -202,6 +204,8 @@ int fdfd_solve(fdfd_handle *h, const double *b, double *x, int32_t nrhs,
  * after the solve completes. */
 int fdfd_solve_dev(fdfd_handle *h, const void *b, void *x,
                    const fdfd_solve_opts *opts, fdfd_stats *stats);
+/* Defaults: BiCGStab(4), mixed precision, tol 1e-6, maxit 200000, δ 0.1,
+ * check_every 50, CUDA graphs on. */
 void fdfd_default_opts(fdfd_solve_opts *opts);
 
 /* ---- field post-processing -------------------------------------------------

@@ -24,7 +24,7 @@ FDFD_ERR_TIMEOUT = 9
 FDFD_C128, FDFD_C64 = 0, 1
 FDFD_EE, FDFD_HH = 0, 1
 FDFD_PREC_FP64, FDFD_PREC_MIXED = 0, 1
-FDFD_BICGSTAB, FDFD_COCG = 0, 1
+FDFD_BICGSTAB, FDFD_COCG, FDFD_BICGSTABL = 0, 1, 2
 FDFD_SHAPE_SPHERE, FDFD_SHAPE_BOX, FDFD_SHAPE_CYLZ = 0, 1, 2
 FDFD_SLICE_NONE, FDFD_SLICE_TE, FDFD_SLICE_TM = 0, 1, 2
 
@@ -49,7 +49,7 @@ class fdfd_design(C.Structure):
 class fdfd_solve_opts(C.Structure):
     _fields_ = [("method", C.c_int32), ("precision", C.c_int32), ("tol", C.c_double), ("maxit", C.c_int64),
                 ("delta", C.c_double), ("x0_given", C.c_int32), ("check_every", C.c_int32),
-                ("transpose", C.c_int32), ("use_graph", C.c_int32)]
+                ("transpose", C.c_int32), ("use_graph", C.c_int32), ("ell", C.c_int32)]
 
 
 class fdfd_stats(C.Structure):

@@ -1,0 +1,333 @@
+// BiCGStab(ℓ) (Sleijpen & Fokkema, ETNA 1, 1993), ℓ ≤ 4, for the same
+// systems as BiCGSTAB: ℓ BiCG steps followed by a minimal-residual
+// polynomial of degree ℓ.  On the FDFD operator, whose spectrum has large
+// imaginary parts, the degree-1 polynomial of BiCGSTAB stalls where the
+// degree-ℓ one does not; it needs markedly fewer operator applications in
+// both precisions, for about 1.3× the vector traffic per application.
+//
+// One cycle = 4ℓ + 2 kernels, all reading their scalars from device memory
+// (so a batch of cycles replays as one CUDA graph):
+//   for j = 0 … ℓ−1:
+//     u_i = r_i − β u_i (i ≤ j)                      k_bl_u
+//     u_{j+1} = A u_j, γ = (r̂, u_{j+1}), α = ρ/γ     operator, EPI_DOT_AUX + FIN_ALPHA
+//     r_i −= α u_{i+1} (i ≤ j), x += α u_0           k_bl_r
+//     r_{j+1} = A r_j [, ρ₁ = (r̂, r_{j+1}), β]       operator, EPI_DOT_AUX + FIN_BL_RHO
+//   Gram matrix of r_0 … r_ℓ and the minimal-residual coefficients
+//   (modified Gram–Schmidt carried out on the Gram matrix)    k_bl_gram
+//   x, r_0, u_0 closing update, (r̂, r_0), ‖r_0‖², stop tests  k_bl_fin + FIN_BL_CYCLE
+// Vectors and products are in the solve's inner precision; every sum
+// across threads and blocks is FP64, in a fixed order.
+#include "krylov_fin.cuh"
+
+namespace fdfd {
+
+namespace {
+
+constexpr int VB = 256;
+constexpr int RED_BLOCKS = 152 * 4;
+constexpr int LMAX = 4;
+
+template <typename C>
+struct VSet {
+  C *v[LMAX + 1];
+};
+
+template <typename R>
+__device__ __forceinline__ typename CT<R>::C tocr(double2 v) {
+  return mk(R(v.x), R(v.y));
+}
+
+__device__ __forceinline__ double2 conjd(double2 a) { return make_double2(a.x, -a.y); }
+__device__ __forceinline__ double2 addd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 subd(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 scd(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+
+template <typename R>
+__device__ __forceinline__ long long vstride() { return (long long)gridDim.x * VB; }
+
+// u_i = r_i − β u_i for i = 0 … j
+template <typename R>
+__global__ void __launch_bounds__(VB) k_bl_u(VSet<typename CT<R>::C> r, VSet<typename CT<R>::C> u, int j, long long n,
+                                             const KScalars *sc) {
+  using C = typename CT<R>::C;
+  if (sc->done) return;
+  const C be = tocr<R>(sc->beta);
+  for (long long e = blockIdx.x * (long long)VB + threadIdx.x; e < n; e += vstride<R>()) {
+    for (int i = 0; i <= j; ++i) u.v[i][e] = csub(r.v[i][e], cmul(be, u.v[i][e]));
+  }
+}
+
+// r_i −= α u_{i+1} for i = 0 … j;  x += α u_0
+template <typename R>
+__global__ void __launch_bounds__(VB) k_bl_r(VSet<typename CT<R>::C> r, VSet<typename CT<R>::C> u,
+                                             typename CT<R>::C *x, int j, long long n, const KScalars *sc) {
+  using C = typename CT<R>::C;
+  if (sc->done) return;
+  const C al = tocr<R>(sc->alpha);
+  for (long long e = blockIdx.x * (long long)VB + threadIdx.x; e < n; e += vstride<R>()) {
+    for (int i = 0; i <= j; ++i) r.v[i][e] = csub(r.v[i][e], cmul(al, u.v[i + 1][e]));
+    x[e] = cadd(x[e], cmul(al, u.v[0][e]));
+  }
+}
+
+// Sum NV complex values over the block, write the block's partials, and
+// return true in the block that arrives last (which then holds the grid
+// sums, in block order, in `tot`).
+template <int NV>
+__device__ bool block_sums_last(double2 (&v)[NV], RedBuf red, double2 (&tot)[NV]) {
+  __shared__ double2 wred[VB / 32][NV];
+  __shared__ bool last;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+#pragma unroll
+  for (int q = 0; q < NV; ++q)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      v[q].x += __shfl_xor_sync(0xffffffffu, v[q].x, o);
+      v[q].y += __shfl_xor_sync(0xffffffffu, v[q].y, o);
+    }
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < NV; ++q) wred[wid][q] = v[q];
+  __syncthreads();
+  if (tid < NV) {
+    double2 s = make_double2(0, 0);
+    for (int w = 0; w < VB / 32; ++w) s = addd(s, wred[w][tid]);
+    red.part[(long long)NV * blockIdx.x + tid] = s;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    __threadfence();
+    const unsigned prev = atomicAdd(red.count, 1u);
+    last = prev == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  if (tid < NV) {
+    double2 s = make_double2(0, 0);
+    for (unsigned b = 0; b < gridDim.x; ++b) s = addd(s, __ldcg(&red.part[(long long)NV * b + tid]));
+    tot[tid] = s;  // tot lives in shared memory of the caller
+  }
+  __syncthreads();
+  if (tid == 0) *red.count = 0u;
+  return true;
+}
+
+// Gram matrix of r_0 … r_L — (r_i, r_j) for 1 ≤ i ≤ j ≤ L, then (r_i, r_0)
+// for 1 ≤ i ≤ L — and, in the last block, the minimal-residual step.
+template <typename R, int L>
+__global__ void __launch_bounds__(VB) k_bl_gram(VSet<typename CT<R>::C> r, long long n, RedBuf red, KScalars *sc) {
+  using C = typename CT<R>::C;
+  constexpr int NV = L * (L + 1) / 2 + L;
+  if (sc->done) return;
+  R ar[NV], ai[NV];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) ar[q] = ai[q] = R(0);
+  for (long long e = blockIdx.x * (long long)VB + threadIdx.x; e < n; e += vstride<R>()) {
+    C v[L + 1];
+#pragma unroll
+    for (int i = 0; i <= L; ++i) v[i] = r.v[i][e];
+    int q = 0;
+#pragma unroll
+    for (int j = 1; j <= L; ++j)
+#pragma unroll
+      for (int i = 1; i <= j; ++i, ++q) {
+        const C d = cdotc(v[i], v[j]);
+        ar[q] += d.x;
+        ai[q] += d.y;
+      }
+#pragma unroll
+    for (int i = 1; i <= L; ++i, ++q) {
+      const C d = cdotc(v[i], v[0]);
+      ar[q] += d.x;
+      ai[q] += d.y;
+    }
+  }
+  double2 acc[NV];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) acc[q] = make_double2((double)ar[q], (double)ai[q]);
+  __shared__ double2 tot[NV];
+  if (!block_sums_last<NV>(acc, red, tot)) return;
+  if (threadIdx.x != 0) return;
+  // Gram matrix G[i][j] = (r_i, r_j), i, j ≥ 1, and g0[i] = (r_i, r_0)
+  double2 G[L + 1][L + 1], g0[L + 1];
+  {
+    int q = 0;
+    for (int j = 1; j <= L; ++j)
+      for (int i = 1; i <= j; ++i, ++q) {
+        G[i][j] = tot[q];
+        G[j][i] = conjd(tot[q]);
+      }
+    for (int i = 1; i <= L; ++i, ++q) g0[i] = tot[q];
+  }
+  // orthogonalised r̂_j = Σ_k Lc[j][k] r_k (k ≤ j); τ, σ, γ' as in MGS
+  double2 Lc[L + 1][L + 1], tau[L + 1][L + 1], gp[L + 1], gam[L + 1], gpp[L + 1];
+  double sig[L + 1];
+  for (int a = 0; a <= L; ++a)
+    for (int b = 0; b <= L; ++b) Lc[a][b] = tau[a][b] = make_double2(0, 0);
+  for (int j = 1; j <= L; ++j) {
+    Lc[j][j] = make_double2(1, 0);
+    for (int i = 1; i < j; ++i) {
+      double2 d = make_double2(0, 0);  // (r̂_i, r_j)
+      for (int k = 1; k <= i; ++k) d = addd(d, dcmul(conjd(Lc[i][k]), G[k][j]));
+      tau[i][j] = scd(d, 1.0 / sig[i]);
+      for (int k = 1; k <= i; ++k) Lc[j][k] = subd(Lc[j][k], dcmul(tau[i][j], Lc[i][k]));
+    }
+    double s = 0.0;  // (r̂_j, r̂_j)
+    double2 g = make_double2(0, 0);  // (r̂_j, r_0)
+    for (int k = 1; k <= j; ++k) {
+      for (int m = 1; m <= j; ++m) s += dcmul(dcmul(conjd(Lc[j][k]), Lc[j][m]), G[k][m]).x;
+      g = addd(g, dcmul(conjd(Lc[j][k]), g0[k]));
+    }
+    if (!(s > 0.0) || !isfinite(s)) {
+      sc->done = 1;
+      sc->reason = isfinite(s) ? 3 : 4;
+      return;
+    }
+    sig[j] = s;
+    gp[j] = scd(g, 1.0 / s);
+  }
+  gam[L] = gp[L];
+  for (int j = L - 1; j >= 1; --j) {
+    double2 t = gp[j];
+    for (int i = j + 1; i <= L; ++i) t = subd(t, dcmul(tau[j][i], gam[i]));
+    gam[j] = t;
+  }
+  for (int j = 1; j < L; ++j) {
+    double2 t = gam[j + 1];
+    for (int i = j + 1; i < L; ++i) t = addd(t, dcmul(tau[j][i], gam[i + 1]));
+    gpp[j] = t;
+  }
+  // closing update in terms of the original r_k
+  for (int k = 0; k <= LMAX; ++k) sc->cx[k] = sc->cr[k] = sc->cu[k] = make_double2(0, 0);
+  sc->cx[0] = gam[1];
+  for (int k = 1; k <= L; ++k) {
+    double2 cx = make_double2(0, 0), cr = make_double2(0, 0);
+    for (int j = k; j < L; ++j) cx = addd(cx, dcmul(gpp[j], Lc[j][k]));
+    for (int j = k; j <= L; ++j) cr = subd(cr, dcmul(gp[j], Lc[j][k]));
+    sc->cx[k] = cx;
+    sc->cr[k] = cr;
+    sc->cu[k] = make_double2(-gam[k].x, -gam[k].y);
+  }
+  sc->omega = gam[L];
+}
+
+// x += Σ cx_k r_k ; r_0 += Σ cr_k r_k ; u_0 += Σ cu_k u_k ; then (r̂, r_0)
+// and ‖r_0‖² → FIN_BL_CYCLE
+template <typename R, int L>
+__global__ void __launch_bounds__(VB) k_bl_fin(VSet<typename CT<R>::C> r, VSet<typename CT<R>::C> u,
+                                               typename CT<R>::C *x, const typename CT<R>::C *__restrict__ rh,
+                                               long long n, RedBuf red, KScalars *sc) {
+  using C = typename CT<R>::C;
+  if (sc->done) return;
+  C cx[L + 1], cr[L + 1], cu[L + 1];
+#pragma unroll
+  for (int k = 0; k <= L; ++k) {
+    cx[k] = tocr<R>(sc->cx[k]);
+    cr[k] = tocr<R>(sc->cr[k]);
+    cu[k] = tocr<R>(sc->cu[k]);
+  }
+  Acc<R> a0r, a0i, a1;
+  for (long long e = blockIdx.x * (long long)VB + threadIdx.x; e < n; e += vstride<R>()) {
+    C rv[L + 1];
+#pragma unroll
+    for (int k = 0; k <= L; ++k) rv[k] = r.v[k][e];
+    C xe = x[e], r0 = rv[0], u0 = u.v[0][e];
+#pragma unroll
+    for (int k = 0; k <= L; ++k) xe = cadd(xe, cmul(cx[k], rv[k]));
+#pragma unroll
+    for (int k = 1; k <= L; ++k) {
+      r0 = cadd(r0, cmul(cr[k], rv[k]));
+      u0 = cadd(u0, cmul(cu[k], u.v[k][e]));
+    }
+    x[e] = xe;
+    r.v[0][e] = r0;
+    u.v[0][e] = u0;
+    const C d = cdotc(rh[e], r0);
+    a0r.add(d.x);
+    a0i.add(d.y);
+    a1.add(r0.x * r0.x + r0.y * r0.y);
+  }
+  block_reduce_finalise<VB>(make_double2(a0r.get(), a0i.get()), make_double2(a1.get(), 0.0), red, FIN_BL_CYCLE, sc);
+}
+
+// (r̂, r_0) for a replaced residual → FIN_BL_REDO
+template <typename R>
+__global__ void __launch_bounds__(VB) k_bl_redo(const typename CT<R>::C *__restrict__ rh,
+                                                const typename CT<R>::C *__restrict__ r0, long long n, RedBuf red,
+                                                KScalars *sc) {
+  using C = typename CT<R>::C;
+  Acc<R> a0r, a0i;
+  for (long long e = blockIdx.x * (long long)VB + threadIdx.x; e < n; e += vstride<R>()) {
+    const C d = cdotc(rh[e], r0[e]);
+    a0r.add(d.x);
+    a0i.add(d.y);
+  }
+  block_reduce_finalise<VB>(make_double2(a0r.get(), a0i.get()), make_double2(0.0, 0.0), red, FIN_BL_REDO, sc);
+}
+
+}  // namespace
+
+template <typename R>
+static VSet<typename CT<R>::C> vset(typename CT<R>::C *const *v, int count) {
+  VSet<typename CT<R>::C> s{};
+  for (int i = 0; i < count && i <= LMAX; ++i) s.v[i] = v[i];
+  return s;
+}
+
+template <typename R, int L>
+static int bl_cycle_t(fdfd_handle *h, typename CT<R>::C *x, typename CT<R>::C *rh, typename CT<R>::C *const *r,
+                      typename CT<R>::C *const *u, long long n, KScalars *sc, bool tr) {
+  const VSet<typename CT<R>::C> rs = vset<R>(r, L + 1), us = vset<R>(u, L + 1);
+  int rc;
+  for (int j = 0; j < L; ++j) {
+    k_bl_u<R><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, j, n, sc);
+    h->launches++;
+    if ((rc = cuda_check(h, cudaGetLastError(), "k_bl_u"))) return rc;
+    if ((rc = launch_apply_fin<R>(h, u[j], u[j + 1], EPI_DOT_AUX, rh, FIN_ALPHA, sc, tr))) return rc;
+    k_bl_r<R><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, j, n, sc);
+    h->launches++;
+    if ((rc = cuda_check(h, cudaGetLastError(), "k_bl_r"))) return rc;
+    if (j + 1 < L) rc = launch_apply_fin<R>(h, r[j], r[j + 1], EPI_DOT_AUX, rh, FIN_BL_RHO, sc, tr);
+    else rc = launch_apply_fin<R>(h, r[j], r[j + 1], EPI_STORE, nullptr, FIN_NONE, sc, tr);
+    if (rc) return rc;
+  }
+  if ((rc = ensure_red(h, 8 * RED_BLOCKS))) return rc;
+  k_bl_gram<R, L><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, n, h->red, sc);
+  h->launches++;
+  if ((rc = cuda_check(h, cudaGetLastError(), "k_bl_gram"))) return rc;
+  k_bl_fin<R, L><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, rh, n, h->red, sc);
+  h->launches++;
+  return cuda_check(h, cudaGetLastError(), "k_bl_fin");
+}
+
+// One BiCGStab(ℓ) cycle (2ℓ operator applications).
+template <typename R>
+int bl_cycle(fdfd_handle *h, typename CT<R>::C *x, typename CT<R>::C *rh, typename CT<R>::C *const *r,
+             typename CT<R>::C *const *u, long long n, int ell, KScalars *sc, bool tr) {
+  switch (ell) {
+    case 1: return bl_cycle_t<R, 1>(h, x, rh, r, u, n, sc, tr);
+    case 2: return bl_cycle_t<R, 2>(h, x, rh, r, u, n, sc, tr);
+    case 3: return bl_cycle_t<R, 3>(h, x, rh, r, u, n, sc, tr);
+    case 4: return bl_cycle_t<R, 4>(h, x, rh, r, u, n, sc, tr);
+  }
+  return set_error(h, FDFD_ERR_ARG, "BiCGStab(l) needs 1 <= l <= 4");
+}
+
+template <typename R>
+int bl_redo(fdfd_handle *h, const typename CT<R>::C *rh, const typename CT<R>::C *r0, long long n, KScalars *sc) {
+  int rc = ensure_red(h, RED_BLOCKS);
+  if (rc) return rc;
+  k_bl_redo<R><<<RED_BLOCKS, VB, 0, h->stream>>>(rh, r0, n, h->red, sc);
+  h->launches++;
+  return cuda_check(h, cudaGetLastError(), "k_bl_redo");
+}
+
+template int bl_cycle<float>(fdfd_handle *, float2 *, float2 *, float2 *const *, float2 *const *, long long, int,
+                             KScalars *, bool);
+template int bl_cycle<double>(fdfd_handle *, double2 *, double2 *, double2 *const *, double2 *const *, long long,
+                              int, KScalars *, bool);
+template int bl_redo<float>(fdfd_handle *, const float2 *, const float2 *, long long, KScalars *);
+template int bl_redo<double>(fdfd_handle *, const double2 *, const double2 *, long long, KScalars *);
+
+}  // namespace fdfd

@@ -290,7 +290,7 @@ const char *fdfd_last_error(const fdfd_handle *h) {
 void fdfd_default_opts(fdfd_solve_opts *o) {
   if (!o) return;
   std::memset(o, 0, sizeof(*o));
-  o->method = FDFD_BICGSTAB;
+  o->method = FDFD_BICGSTABL;  // BiCGStab(4): the fewest operator applications on these systems
   o->precision = FDFD_PREC_MIXED;
   o->tol = 1e-6;
   o->maxit = 200000;
@@ -299,6 +299,7 @@ void fdfd_default_opts(fdfd_solve_opts *o) {
   o->check_every = 50;
   o->transpose = 0;
   o->use_graph = 1;
+  o->ell = 4;
 }
 
 int fdfd_create(const fdfd_desc *d, fdfd_handle **out) {
@@ -592,7 +593,10 @@ static int check_opts(fdfd_handle *h, const fdfd_solve_opts *o) {
   if (!o) return set_error(h, FDFD_ERR_ARG, "null options");
   if (o->precision != FDFD_PREC_FP64 && o->precision != FDFD_PREC_MIXED)
     return set_error(h, FDFD_ERR_ARG, "bad precision");
-  if (o->method != FDFD_BICGSTAB && o->method != FDFD_COCG) return set_error(h, FDFD_ERR_ARG, "bad method");
+  if (o->method != FDFD_BICGSTAB && o->method != FDFD_COCG && o->method != FDFD_BICGSTABL)
+    return set_error(h, FDFD_ERR_ARG, "bad method");
+  if (o->method == FDFD_BICGSTABL && (o->ell < 1 || o->ell > 4))
+    return set_error(h, FDFD_ERR_ARG, "BiCGStab(l) needs 1 <= ell <= 4");
   if (!(o->tol > 0.0) || o->maxit < 1) return set_error(h, FDFD_ERR_ARG, "bad tol/maxit");
   if (o->precision == FDFD_PREC_MIXED && !(o->delta > 0.0 && o->delta < 1.0))
     return set_error(h, FDFD_ERR_ARG, "delta must be in (0, 1)");
@@ -651,7 +655,7 @@ int fdfd_eps_grad_dev(fdfd_handle *h, const void *e, const void *g, void *lam, d
   if (!h || !e || !g || !lam || !grad) return set_error(h, FDFD_ERR_ARG, "null argument");
   int rc = check_opts(h, opts);
   if (rc) return rc;
-  if (opts->method != FDFD_BICGSTAB) return set_error(h, FDFD_ERR_UNSUPPORTED, "the adjoint solve uses BiCGSTAB");
+  if (opts->method == FDFD_COCG) return set_error(h, FDFD_ERR_UNSUPPORTED, "the adjoint solve uses BiCGSTAB or BiCGStab(l)");
   if (h->ft != FDFD_EE) return set_error(h, FDFD_ERR_UNSUPPORTED, "the ε gradient is for the E formulation");
   if (!transpose_ok(h)) return set_error(h, FDFD_ERR_UNSUPPORTED, "adjoint with a Bloch phase");
   cudaSetDevice(h->dev);
@@ -665,7 +669,7 @@ int fdfd_eps_grad(fdfd_handle *h, const double *e, const double *g, double *grad
   if (!h || !e || !g || !grad) return set_error(h, FDFD_ERR_ARG, "null argument");
   int rc = check_opts(h, opts);
   if (rc) return rc;
-  if (opts->method != FDFD_BICGSTAB) return set_error(h, FDFD_ERR_UNSUPPORTED, "the adjoint solve uses BiCGSTAB");
+  if (opts->method == FDFD_COCG) return set_error(h, FDFD_ERR_UNSUPPORTED, "the adjoint solve uses BiCGSTAB or BiCGStab(l)");
   if (h->ft != FDFD_EE) return set_error(h, FDFD_ERR_UNSUPPORTED, "the ε gradient is for the E formulation");
   if (!transpose_ok(h)) return set_error(h, FDFD_ERR_UNSUPPORTED, "adjoint with a Bloch phase");
   cudaSetDevice(h->dev);

@@ -89,6 +89,10 @@ struct KScalars {
   int done;              // 1: later kernels of the batch are no-ops
   int reason;            // 1 recursive converged, 2 reliable update due, 3 breakdown, 4 nonfinite
   long long iter;
+  // BiCGStab(ℓ), ℓ ≤ 4: −ω·ρ of the last cycle end, and the coefficients of
+  // the cycle's closing update x += Σ cx_k r_k, r₀ += Σ cr_k r_k, u₀ += Σ cu_k u_k
+  double2 rho_pre;
+  double2 cx[5], cr[5], cu[5];
 };
 
 struct Workspace;  // solver vectors (solver.cu)

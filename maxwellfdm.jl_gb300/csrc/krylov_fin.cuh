@@ -19,6 +19,9 @@ enum FinMode : int {
   FIN_RESID = 4,   // ‖b − A x‖² into dot0.x (reliable update / final check)
   FIN_COCG_A = 5,  // COCG: α = ρ / (pᵀ q)
   FIN_COCG_R = 6,  // COCG: ρ' = rᵀ r, β = ρ'/ρ, ‖r‖², stop tests
+  FIN_BL_RHO = 7,    // BiCGStab(ℓ) inside a cycle: ρ₁ = (r̂, r_j), β = α ρ₁/ρ₀, ρ₀ = ρ₁
+  FIN_BL_CYCLE = 8,  // BiCGStab(ℓ) cycle end: ρ₀ = −ω ρ₀, then as FIN_BL_RHO; ‖r₀‖², stop tests
+  FIN_BL_REDO = 9,   // after a replaced residual: ρ₁ = (r̂, r₀) against the stored −ω ρ₀
 };
 
 __device__ __forceinline__ double2 dcdiv(double2 a, double2 b) {
@@ -68,6 +71,23 @@ __device__ inline void finalise(int mode, KScalars *sc, double2 d0, double2 d1) 
       if (!dfinite(d0)) { sc->done = 1; sc->reason = 4; break; }
       if (d0.x == 0.0 && d0.y == 0.0) { sc->done = 1; sc->reason = 3; break; }
       sc->alpha = dcdiv(sc->rho, d0);
+      break;
+    }
+    case FIN_BL_RHO:
+    case FIN_BL_REDO:
+    case FIN_BL_CYCLE: {
+      if (mode == FIN_BL_CYCLE) sc->rho_pre = make_double2(-(sc->omega.x * sc->rho.x - sc->omega.y * sc->rho.y),
+                                                          -(sc->omega.x * sc->rho.y + sc->omega.y * sc->rho.x));
+      const double2 rho0 = mode == FIN_BL_RHO ? sc->rho : sc->rho_pre;
+      if (!dfinite(d0)) { sc->done = 1; sc->reason = 4; break; }
+      if (rho0.x == 0.0 && rho0.y == 0.0) {
+        if (mode == FIN_BL_CYCLE) stop_tests(sc, d1.x);
+        if (!sc->done) { sc->done = 1; sc->reason = 3; }
+        break;
+      }
+      sc->beta = dcmul(sc->alpha, dcdiv(d0, rho0));
+      sc->rho = d0;
+      if (mode == FIN_BL_CYCLE) stop_tests(sc, d1.x);
       break;
     }
     case FIN_COCG_R: {

@@ -14,6 +14,7 @@
 // The scalars of the recurrences live on the device (KScalars); a batch of
 // `check_every` iterations is one CUDA graph replay with no host sync;
 // kernels become no-ops once a stop condition is reached inside a batch.
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -50,6 +51,11 @@ int accum64(fdfd_handle *, double2 *, double2 *, long long);
 int demote(fdfd_handle *, float2 *, const double2 *, long long);
 int promote(fdfd_handle *, double2 *, const float2 *, long long);
 int build_weights(fdfd_handle *h, double2 *w64, float2 *w32, double2 *d64, float2 *d32);
+template <typename R>
+int bl_cycle(fdfd_handle *, typename CT<R>::C *, typename CT<R>::C *, typename CT<R>::C *const *,
+             typename CT<R>::C *const *, long long, int, KScalars *, bool);
+template <typename R>
+int bl_redo(fdfd_handle *, const typename CT<R>::C *, const typename CT<R>::C *, long long, KScalars *);
 
 #define TRY(x)              \
   do {                      \
@@ -60,15 +66,16 @@ int build_weights(fdfd_handle *h, double2 *w64, float2 *w32, double2 *d64, float
 struct Workspace {
   long long n = 0;
   double2 *x64 = nullptr, *r64 = nullptr;
-  float2 *f[7] = {nullptr};
-  double2 *d[7] = {nullptr};
+  float2 *f[12] = {nullptr};   // inner vectors: BiCGSTAB 7, COCG 4, BiCGStab(ℓ) 2ℓ+4
+  double2 *d[12] = {nullptr};
   double2 *w64 = nullptr, *dj64 = nullptr;  // COCG: S weights and Jacobi factors 1/diag(A)
   float2 *w32 = nullptr, *dj32 = nullptr;
   KScalars *sc = nullptr, *scu = nullptr;
   KScalars *host = nullptr;  // pinned mirror
-  cudaGraphExec_t gexec[2][2][2] = {};  // [precision][method][transpose]
-  int gbatch[2][2][2] = {};
-  long long gkern[2][2][2] = {};        // kernels per graph replay
+  cudaGraphExec_t gexec[2][3][2] = {};  // [precision][method][transpose]
+  int gbatch[2][3][2] = {};
+  int gell[2][3][2] = {};               // ℓ the BiCGStab(ℓ) graph was captured with
+  long long gkern[2][3][2] = {};        // kernels per graph replay
 };
 
 void free_workspace(fdfd_handle *h) {
@@ -76,7 +83,7 @@ void free_workspace(fdfd_handle *h) {
   if (!ws) return;
   cudaFree(ws->x64);
   cudaFree(ws->r64);
-  for (int i = 0; i < 7; ++i) {
+  for (int i = 0; i < 12; ++i) {
     cudaFree(ws->f[i]);
     cudaFree(ws->d[i]);
   }
@@ -117,7 +124,7 @@ static int alloc(fdfd_handle *h, void **p, size_t bytes, const char *what) {
   return FDFD_OK;
 }
 
-static int ensure_ws(fdfd_handle *h, bool mixed, int method) {
+static int ensure_ws(fdfd_handle *h, bool mixed, int method, int ell) {
   if (!h->ws) {
     h->ws = new Workspace();
     h->ws->n = 3 * h->ncell;
@@ -126,7 +133,7 @@ static int ensure_ws(fdfd_handle *h, bool mixed, int method) {
   const size_t n = (size_t)ws->n;
   TRY(alloc(h, (void **)&ws->x64, n * sizeof(double2), "x64"));
   TRY(alloc(h, (void **)&ws->r64, n * sizeof(double2), "r64"));
-  const int nv = (method == FDFD_COCG) ? 4 : 7;
+  const int nv = method == FDFD_COCG ? 4 : method == FDFD_BICGSTABL ? 2 * ell + 4 : 7;
   for (int i = 0; i < nv; ++i) {
     if (mixed) TRY(alloc(h, (void **)&ws->f[i], n * sizeof(float2), "inner vector (c64)"));
     else TRY(alloc(h, (void **)&ws->d[i], n * sizeof(double2), "inner vector (c128)"));
@@ -217,6 +224,19 @@ static int cocg_iter(fdfd_handle *h, Workspace *ws, bool tr) {
   return FDFD_OK;
 }
 
+// One BiCGStab(ℓ) cycle.  Vectors: 0 x (correction), 1 r̂, 2 … 2+ℓ r_0 … r_ℓ,
+// 3+ℓ … 3+2ℓ u_0 … u_ℓ.
+template <typename R>
+static int bl_iter(fdfd_handle *h, Workspace *ws, int ell, bool tr) {
+  using C = typename CT<R>::C;
+  C *r[5], *u[5];
+  for (int i = 0; i <= ell; ++i) {
+    r[i] = vec<R>(ws, 2 + i);
+    u[i] = vec<R>(ws, 3 + ell + i);
+  }
+  return bl_cycle<R>(h, vec<R>(ws, 0), vec<R>(ws, 1), r, u, ws->n, ell, ws->sc, tr);
+}
+
 // ρ = rᵀ S D⁻¹ r of the current residual (q is used as scratch for D⁻¹ r)
 template <typename R>
 static int cocg_rho(fdfd_handle *h, Workspace *ws, double2 *rho) {
@@ -230,26 +250,28 @@ static int cocg_rho(fdfd_handle *h, Workspace *ws, double2 *rho) {
 }
 
 template <typename R>
-static int run_batch(fdfd_handle *h, Workspace *ws, int method, bool tr, int batch, bool use_graph) {
+static int run_batch(fdfd_handle *h, Workspace *ws, int method, int ell, bool tr, int batch, bool use_graph) {
   const int pi = sizeof(R) == 4 ? 1 : 0;
-  const int mi = method == FDFD_COCG ? 1 : 0;
+  const int mi = method == FDFD_COCG ? 1 : method == FDFD_BICGSTABL ? 2 : 0;
   const int ti = tr ? 1 : 0;
   auto body = [&]() -> int {
     for (int i = 0; i < batch; ++i) {
       if (method == FDFD_COCG) TRY(cocg_iter<R>(h, ws, tr));
+      else if (method == FDFD_BICGSTABL) TRY(bl_iter<R>(h, ws, ell, tr));
       else TRY(bicg_iter<R>(h, ws, tr));
     }
     return FDFD_OK;
   };
+  // lazily-sized buffers must exist before any capture (the Gram kernel of
+  // BiCGStab(ℓ) keeps up to 16 partials per block)
+  TRY(ensure_red(h, std::max(apply_blocks(h), method == FDFD_BICGSTABL ? 8 * 152 * 4 : 0)));
   if (!use_graph) return body();
   cudaGraphExec_t &ge = ws->gexec[pi][mi][ti];
-  if (ge && ws->gbatch[pi][mi][ti] != batch) {
+  if (ge && (ws->gbatch[pi][mi][ti] != batch || ws->gell[pi][mi][ti] != ell)) {
     cudaGraphExecDestroy(ge);
     ge = nullptr;
   }
   if (!ge) {
-    // make sure lazily-sized buffers exist before capture
-    TRY(ensure_red(h, apply_blocks(h)));
     cudaGraph_t g;
     TRY(cuda_check(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture"));
     const long long l0 = h->launches;
@@ -263,6 +285,7 @@ static int run_batch(fdfd_handle *h, Workspace *ws, int method, bool tr, int bat
     cudaGraphDestroy(g);
     TRY(cuda_check(h, e, "graph instantiate"));
     ws->gbatch[pi][mi][ti] = batch;
+    ws->gell[pi][mi][ti] = ell;
   }
   h->launches += ws->gkern[pi][mi][ti];
   return cuda_check(h, cudaGraphLaunch(ge, h->stream), "graph launch");
@@ -270,10 +293,29 @@ static int run_batch(fdfd_handle *h, Workspace *ws, int method, bool tr, int bat
 
 // (Re)initialise the inner iteration from the FP64 residual r64.
 template <typename R>
-static int init_inner(fdfd_handle *h, Workspace *ws, int method, double rr, KScalars *hs) {
+static int init_inner(fdfd_handle *h, Workspace *ws, int method, int ell, double rr, KScalars *hs) {
   using C = typename CT<R>::C;
   const long long n = ws->n;
   const size_t bytes = (size_t)n * sizeof(C);
+  if (method == FDFD_BICGSTABL) {
+    // r_0 = r64, r̂ = r_0, u_0 = 0, x = 0; ρ₀ = (r̂, r_0), α = 0 so the first β is 0
+    C *r0 = vec<R>(ws, 2);
+    if constexpr (sizeof(R) == 4) TRY(demote(h, r0, ws->r64, n));
+    else TRY(copy<double>(h, r0, ws->r64, n));
+    TRY(copy<R>(h, vec<R>(ws, 1), r0, n));
+    TRY(cuda_check(h, cudaMemsetAsync(vec<R>(ws, 0), 0, bytes, h->stream), "memset x"));
+    TRY(cuda_check(h, cudaMemsetAsync(vec<R>(ws, 3 + ell), 0, bytes, h->stream), "memset u0"));
+    hs->rho = make_double2(rr, 0.0);
+    hs->alpha = make_double2(0.0, 0.0);
+    hs->omega = make_double2(1.0, 0.0);
+    hs->beta = make_double2(0.0, 0.0);
+    hs->rho_pre = make_double2(-1.0, 0.0);
+    hs->rr = rr;
+    hs->rr_max = rr;
+    hs->done = 0;
+    hs->reason = 0;
+    return FDFD_OK;
+  }
   C *r = vec<R>(ws, 1);
   if constexpr (sizeof(R) == 4) TRY(demote(h, r, ws->r64, n));
   else TRY(copy<double>(h, r, ws->r64, n));
@@ -302,7 +344,8 @@ template <typename R>
 static int solve_impl(fdfd_handle *h, const double2 *b, double2 *x, const fdfd_solve_opts &o, fdfd_stats &st) {
   const bool mixed = sizeof(R) == 4;
   const bool tr = o.transpose != 0;
-  TRY(ensure_ws(h, mixed, o.method));
+  const int ell = o.method == FDFD_BICGSTABL ? o.ell : 1;
+  TRY(ensure_ws(h, mixed, o.method, ell));
   Workspace *ws = h->ws;
   const long long n = ws->n;
   TRY(cuda_check(h, cudaEventRecord(h->ev0, h->stream), "event"));
@@ -338,14 +381,16 @@ static int solve_impl(fdfd_handle *h, const double2 *b, double2 *x, const fdfd_s
   if (rr <= tol2) {
     status = FDFD_OK;
   } else {
-    TRY(init_inner<R>(h, ws, o.method, rr, &hs));
+    TRY(init_inner<R>(h, ws, o.method, ell, rr, &hs));
     TRY(write_scalars(h, ws->sc, &hs));
-    const int batch = o.check_every > 0 ? o.check_every : 50;
+    // a BiCGStab(ℓ) cycle counts as ℓ iterations (2ℓ operator applications)
+    const int per = o.method == FDFD_BICGSTABL ? ell : 1;
+    const int batch = std::max(1, (o.check_every > 0 ? o.check_every : 50) / per);
     const int mv_per_it = o.method == FDFD_COCG ? 1 : 2;
     while (true) {
-      TRY(run_batch<R>(h, ws, o.method, tr, batch, o.use_graph != 0));
+      TRY(run_batch<R>(h, ws, o.method, ell, tr, batch, o.use_graph != 0));
       TRY(read_scalars(h, ws->sc, &hs));
-      iters = hs.iter;
+      iters = hs.iter * per;
       if (hs.done) {
         if (hs.reason == 4) { status = FDFD_ERR_NONFINITE; break; }
         // fold the correction into x64 and recompute the true residual
@@ -358,12 +403,12 @@ static int solve_impl(fdfd_handle *h, const double2 *b, double2 *x, const fdfd_s
         if (hs.reason == 3) {
           if (++restarts > 50) { status = FDFD_ERR_BREAKDOWN; break; }
           const long long it_keep = hs.iter;
-          TRY(init_inner<R>(h, ws, o.method, rr, &hs));
+          TRY(init_inner<R>(h, ws, o.method, ell, rr, &hs));
           hs.iter = it_keep;
         } else {
           // reliable update: replace the recursive residual, keep the Krylov state
           using C = typename CT<R>::C;
-          C *r = vec<R>(ws, 1);
+          C *r = vec<R>(ws, o.method == FDFD_BICGSTABL ? 2 : 1);
           if constexpr (sizeof(R) == 4) TRY(demote(h, r, ws->r64, n));
           else TRY(copy<double>(h, r, ws->r64, n));
           hs.rr = rr;
@@ -373,6 +418,11 @@ static int solve_impl(fdfd_handle *h, const double2 *b, double2 *x, const fdfd_s
           if (o.method == FDFD_COCG) {
             // COCG's ρ = rᵀ S D⁻¹ r must describe the replaced residual
             TRY(cocg_rho<R>(h, ws, &hs.rho));
+          } else if (o.method == FDFD_BICGSTABL) {
+            // ρ₁ = (r̂, r_0) and β of the next cycle for the replaced r_0
+            TRY(write_scalars(h, ws->sc, &hs));
+            TRY(bl_redo<R>(h, vec<R>(ws, 1), r, n, ws->sc));
+            TRY(read_scalars(h, ws->sc, &hs));
           }
         }
         TRY(write_scalars(h, ws->sc, &hs));

@@ -27,7 +27,7 @@ struct FDFDDesc
 end
 
 Base.@kwdef struct SolveOpts
-    method::Int32 = 0          # 0 BiCGSTAB, 1 COCG (FP64 only)
+    method::Int32 = 2          # 0 BiCGSTAB, 1 COCG (FP64 only), 2 BiCGStab(ℓ) (default)
     precision::Int32 = 1       # 0 FP64, 1 mixed (complex64 + FP64 reliable updates)
     tol::Float64 = 1e-6
     maxit::Int64 = 200000
@@ -36,6 +36,7 @@ Base.@kwdef struct SolveOpts
     check_every::Int32 = 50
     transpose::Int32 = 0
     use_graph::Int32 = 1
+    ell::Int32 = 4             # ℓ of BiCGStab(ℓ)
 end
 
 struct SolveStats
@@ -121,7 +122,7 @@ Base.:\(A::FDFDOperator, b::Vector{ComplexF64}) = ldiv!(zeros(ComplexF64, length
 function solve_pullback(A::FDFDOperator, e::Vector{ComplexF64}, g::Vector{ComplexF64}; opts::SolveOpts=SolveOpts())
     λ = zeros(ComplexF64, length(g))
     o = SolveOpts(opts.method, opts.precision, opts.tol, opts.maxit, opts.delta, 0, opts.check_every, 1,
-                  opts.use_graph)
+                  opts.use_graph, opts.ell)
     solve!(λ, A, g; opts=o)
     return λ
 end

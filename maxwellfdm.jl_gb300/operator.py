@@ -174,17 +174,18 @@ class FDFDOperator:
         return out.value
 
     # ---------------------------------------------------------------- solve
-    def solve(self, b, tol=1e-6, precision="mixed", method="bicgstab", maxit=200000, x0=None, delta=0.1,
-              check_every=50, transpose=False, use_graph=True):
+    def solve(self, b, tol=1e-6, precision="mixed", method="bicgstabl", maxit=200000, x0=None, delta=0.1,
+              check_every=50, transpose=False, use_graph=True, ell=4):
         """x = A \\ b to a true relative residual ``tol``.  b may hold several
-        right-hand sides as rows of a 2D array.  Returns (x, [stats])."""
+        right-hand sides as rows of a 2D array.  method: "bicgstab", "bicgstabl"
+        (BiCGStab(ℓ), ℓ = ell) or "cocg".  Returns (x, [stats])."""
         b = np.ascontiguousarray(b, dtype=np.complex128)
         nrhs = 1 if b.ndim == 1 else b.shape[0]
         b2 = b.reshape(nrhs, -1)
         if b2.shape[1] != self.n:
             raise ValueError("b has the wrong length")
         x = np.zeros_like(b2) if x0 is None else np.ascontiguousarray(x0, np.complex128).reshape(nrhs, -1).copy()
-        o = self._opts(tol, precision, method, maxit, x0 is not None, delta, check_every, transpose, use_graph)
+        o = self._opts(tol, precision, method, maxit, x0 is not None, delta, check_every, transpose, use_graph, ell)
         st = (_lib.fdfd_stats * nrhs)()
         rc = self._lib.fdfd_solve(self._h, dptr(b2), dptr(x), nrhs, C.byref(o), st)
         stats = [s.as_dict() for s in st]
@@ -197,9 +198,10 @@ class FDFDOperator:
 
     def solve_dev(self, b_ptr, x_ptr, **kw):
         """Solve with complex128 device buffers (already resident in HBM)."""
-        o = self._opts(kw.get("tol", 1e-6), kw.get("precision", "mixed"), kw.get("method", "bicgstab"),
+        o = self._opts(kw.get("tol", 1e-6), kw.get("precision", "mixed"), kw.get("method", "bicgstabl"),
                        kw.get("maxit", 200000), kw.get("x0_given", False), kw.get("delta", 0.1),
-                       kw.get("check_every", 50), kw.get("transpose", False), kw.get("use_graph", True))
+                       kw.get("check_every", 50), kw.get("transpose", False), kw.get("use_graph", True),
+                       kw.get("ell", 4))
         st = _lib.fdfd_stats()
         self._check(self._lib.fdfd_solve_dev(self._h, C.c_void_p(b_ptr), C.c_void_p(x_ptr), C.byref(o),
                                              C.byref(st)))
@@ -230,7 +232,8 @@ class FDFDOperator:
         return out
 
     # ---------------------------------------------------------------- adjoint
-    def eps_grad(self, e, g, tol=1e-8, precision="fp64", maxit=200000, delta=0.1, check_every=50, use_graph=True):
+    def eps_grad(self, e, g, tol=1e-8, precision="fp64", maxit=200000, delta=0.1, check_every=50, use_graph=True,
+                 method="bicgstabl", ell=4):
         """dL/dε_cc at every E_c sample for A e = b and g = ∂L/∂e (Wirtinger
         derivative, dL = 2·Re(gᵀ de)): solves Aᵀ λ = g on the GPU and returns
         2·Re(ω²·λ·e) as an (Nx,Ny,Nz,3) array, with the solve's stats."""
@@ -239,7 +242,7 @@ class FDFDOperator:
         if e.size != self.n or g.size != self.n:
             raise ValueError("e and g need 3·Ncell entries")
         grad = np.empty(self.n)
-        o = self._opts(tol, precision, "bicgstab", maxit, False, delta, check_every, True, use_graph)
+        o = self._opts(tol, precision, method, maxit, False, delta, check_every, True, use_graph, ell)
         st = _lib.fdfd_stats()
         self._check(self._lib.fdfd_eps_grad(self._h, dptr(e), dptr(g), dptr(grad), C.byref(o), C.byref(st)))
         return _aos_cell(grad, self.N, self.ncomp_e), st.as_dict()
@@ -257,10 +260,13 @@ class FDFDOperator:
         self._check(self._lib.fdfd_design_grad(self._h, dptr(gv), dptr(out)))
         return np.transpose(out.reshape(ds[2], ds[1], ds[0]), (2, 1, 0))
 
-    def _opts(self, tol, precision, method, maxit, x0_given, delta, check_every, transpose, use_graph):
-        return _lib.default_opts(
+    def _opts(self, tol, precision, method, maxit, x0_given, delta, check_every, transpose, use_graph, ell=4):
+        methods = {"bicgstab": _lib.FDFD_BICGSTAB, "cocg": _lib.FDFD_COCG, "bicgstabl": _lib.FDFD_BICGSTABL}
+        if method not in methods:
+            raise ValueError(f"unknown method {method}")
+        return _lib.default_opts(ell=int(ell),
             tol=float(tol), precision=_lib.FDFD_PREC_MIXED if precision == "mixed" else _lib.FDFD_PREC_FP64,
-            method=_lib.FDFD_COCG if method == "cocg" else _lib.FDFD_BICGSTAB, maxit=int(maxit),
+            method=methods[method], maxit=int(maxit),
             x0_given=int(bool(x0_given)), delta=float(delta), check_every=int(check_every),
             transpose=int(bool(transpose)), use_graph=int(bool(use_graph)))
 

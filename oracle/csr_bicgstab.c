@@ -1,7 +1,7 @@
 /*
  * CPU baseline and test infrastructure (oracle): complex128 CSR sparse
- * matrix-vector product and unpreconditioned BiCGSTAB on all host cores
- * (OpenMP).  The matrix is the oracle's assembled A = Cm*Ce - w^2*Peps
+ * matrix-vector product, unpreconditioned BiCGSTAB and BiCGStab(l)
+ * (Sleijpen & Fokkema 1993) on all host cores (OpenMP).  The matrix is the oracle's assembled A = Cm*Ce - w^2*Peps
  * (the reference's create_A, src/model/model.jl:238-259, which Julia then
  * applies with its single-threaded SparseArrays SpMV and solves with A\b).
  * The recurrence is the one in fdfd_oracle.bicgstab (van der Vorst 1992):
@@ -133,4 +133,120 @@ int64_t csr_bicgstab(int64_t n, const int64_t *indptr, const int32_t *indices, c
 done:
   free(r); free(rh); free(p); free(v); free(s); free(t);
   return it;
+}
+
+static void axpy(int64_t n, cplx a, const cplx *x, cplx *y) { /* y += a x */
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    const cplx t = cmul(a, x[i]);
+    y[i].re += t.re;
+    y[i].im += t.im;
+  }
+}
+static void xpay(int64_t n, const cplx *x, cplx a, cplx *y) { /* y = x + a y */
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    const cplx t = cmul(a, y[i]);
+    y[i].re = x[i].re + t.re;
+    y[i].im = x[i].im + t.im;
+  }
+}
+static inline cplx csub_(cplx a, cplx b) { cplx r = {a.re - b.re, a.im - b.im}; return r; }
+static inline cplx cadd_(cplx a, cplx b) { cplx r = {a.re + b.re, a.im + b.im}; return r; }
+
+/* BiCGStab(l), l <= 8, with the modified Gram-Schmidt minimal-residual part
+ * of the original algorithm; same stopping rule as csr_bicgstab (recursive
+ * residual).  Returns the operator applications done (-1 on allocation
+ * failure). */
+int64_t csr_bicgstabl(int64_t n, const int64_t *indptr, const int32_t *indices, const double *data, const double *b,
+                      double *x, int l, double tol, int64_t maxmv, double *relres) {
+  enum { LM = 8 };
+  if (l < 1 || l > LM) return -1;
+  cplx *r[LM + 1], *u[LM + 1], *rh = malloc(n * sizeof(cplx));
+  int ok = rh != NULL;
+  for (int i = 0; i <= l; ++i) {
+    r[i] = malloc(n * sizeof(cplx));
+    u[i] = calloc(n, sizeof(cplx));
+    ok = ok && r[i] && u[i];
+  }
+  int64_t mv = -1;
+  cplx *X = (cplx *)x;
+  const cplx *B = (const cplx *)b;
+  if (ok) {
+    csr_spmv(n, indptr, indices, data, x, (double *)r[0]);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+      r[0][i].re = B[i].re - r[0][i].re;
+      r[0][i].im = B[i].im - r[0][i].im;
+      rh[i] = r[0][i];
+    }
+    const double nb = nrm2(n, B);
+    cplx rho0 = {1, 0}, alpha = {0, 0}, om = {1, 0};
+    double rel = nrm2(n, r[0]) / nb;
+    mv = 0;
+    while (mv < maxmv && rel >= tol) {
+      const cplx mom = {-om.re, -om.im};
+      rho0 = cmul(mom, rho0);
+      for (int j = 0; j < l; ++j) {
+        const cplx rho1 = dotc(n, rh, r[j]);
+        const cplx beta = cmul(alpha, cdiv(rho1, rho0));
+        rho0 = rho1;
+        const cplx mb = {-beta.re, -beta.im};
+        for (int i = 0; i <= j; ++i) xpay(n, r[i], mb, u[i]);
+        csr_spmv(n, indptr, indices, data, (const double *)u[j], (double *)u[j + 1]);
+        ++mv;
+        alpha = cdiv(rho0, dotc(n, rh, u[j + 1]));
+        const cplx ma = {-alpha.re, -alpha.im};
+        for (int i = 0; i <= j; ++i) axpy(n, ma, u[i + 1], r[i]);
+        csr_spmv(n, indptr, indices, data, (const double *)r[j], (double *)r[j + 1]);
+        ++mv;
+        axpy(n, alpha, u[0], X);
+      }
+      cplx tau[LM + 1][LM + 1], gp[LM + 1], gam[LM + 1], gpp[LM + 1];
+      double sig[LM + 1];
+      for (int j = 1; j <= l; ++j) {
+        for (int i = 1; i < j; ++i) {
+          const cplx d = dotc(n, r[i], r[j]);
+          tau[i][j].re = d.re / sig[i];
+          tau[i][j].im = d.im / sig[i];
+          const cplx mt = {-tau[i][j].re, -tau[i][j].im};
+          axpy(n, mt, r[i], r[j]);
+        }
+        sig[j] = dotc(n, r[j], r[j]).re;
+        const cplx g = dotc(n, r[j], r[0]);
+        gp[j].re = g.re / sig[j];
+        gp[j].im = g.im / sig[j];
+      }
+      gam[l] = gp[l];
+      om = gam[l];
+      for (int j = l - 1; j >= 1; --j) {
+        cplx t = gp[j];
+        for (int i = j + 1; i <= l; ++i) t = csub_(t, cmul(tau[j][i], gam[i]));
+        gam[j] = t;
+      }
+      for (int j = 1; j < l; ++j) {
+        cplx t = gam[j + 1];
+        for (int i = j + 1; i < l; ++i) t = cadd_(t, cmul(tau[j][i], gam[i + 1]));
+        gpp[j] = t;
+      }
+      axpy(n, gam[1], r[0], X);
+      const cplx mg = {-gp[l].re, -gp[l].im}, mgl = {-gam[l].re, -gam[l].im};
+      axpy(n, mg, r[l], r[0]);
+      axpy(n, mgl, u[l], u[0]);
+      for (int j = 1; j < l; ++j) {
+        const cplx mgj = {-gam[j].re, -gam[j].im}, mgpj = {-gp[j].re, -gp[j].im};
+        axpy(n, mgj, u[j], u[0]);
+        axpy(n, gpp[j], r[j], X);
+        axpy(n, mgpj, r[j], r[0]);
+      }
+      rel = nrm2(n, r[0]) / nb;
+    }
+    if (relres) *relres = rel;
+  }
+  free(rh);
+  for (int i = 0; i <= l; ++i) {
+    free(r[i]);
+    free(u[i]);
+  }
+  return mv;
 }

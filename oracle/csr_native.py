@@ -26,6 +26,8 @@ def load():
         lib.csr_spmv.argtypes = [C.c_int64, lp, ip, dp, dp, dp]
         lib.csr_bicgstab.restype = C.c_int64
         lib.csr_bicgstab.argtypes = [C.c_int64, lp, ip, dp, dp, dp, C.c_double, C.c_int64, dp]
+        lib.csr_bicgstabl.restype = C.c_int64
+        lib.csr_bicgstabl.argtypes = [C.c_int64, lp, ip, dp, dp, dp, C.c_int, C.c_double, C.c_int64, dp]
         _lib = lib
     return _lib
 
@@ -62,3 +64,15 @@ class NativeCSR:
         if it < 0:
             raise MemoryError("csr_bicgstab: allocation failed")
         return x, int(it), rel.value
+
+    def bicgstabl(self, b, ell=4, tol=1e-6, maxmv=200000, x0=None):
+        """BiCGStab(ℓ); returns (x, operator applications, recursive relres)."""
+        b = np.ascontiguousarray(b, dtype=np.complex128)
+        x = np.zeros_like(b) if x0 is None else np.ascontiguousarray(x0, dtype=np.complex128).copy()
+        rel = C.c_double()
+        mv = load().csr_bicgstabl(self.n, self._p(self.indptr, C.c_int64), self._p(self.indices, C.c_int32),
+                                  self._p(self.data, C.c_double), self._p(b, C.c_double), self._p(x, C.c_double),
+                                  int(ell), float(tol), int(maxmv), C.byref(rel))
+        if mv < 0:
+            raise MemoryError("csr_bicgstabl: allocation failed or bad l")
+        return x, int(mv), rel.value

@@ -34,7 +34,8 @@ def sysx(oracle):
     return S, b, xd
 
 
-@pytest.mark.parametrize("precision,method", [("fp64", "bicgstab"), ("mixed", "bicgstab"), ("fp64", "cocg")])
+@pytest.mark.parametrize("precision,method", [("fp64", "bicgstab"), ("mixed", "bicgstab"), ("fp64", "cocg"),
+                                              ("fp64", "bicgstabl"), ("mixed", "bicgstabl")])
 def test_solve_matches_direct(pkg, sysx, precision, method):
     S, b, xd = sysx
     A = _op(pkg, S)
@@ -104,4 +105,19 @@ def test_unsupported_cocg_forms_rejected(pkg, sysx):
         with pytest.raises(pkg.FDFDError) as ei:
             A.solve(b, method="cocg", **kw)
         assert ei.value.code == 2
+    A.close()
+
+
+@pytest.mark.parametrize("ell", [1, 2, 3, 4])
+def test_bicgstabl_degrees(pkg, sysx, ell):
+    """BiCGStab(ℓ) for every supported ℓ, mixed precision with reliable
+    updates, transposed as well (the adjoint path)."""
+    S, b, xd = sysx
+    A = _op(pkg, S)
+    for tr in (False, True):
+        x, st = A.solve(b, tol=1e-8, precision="mixed", method="bicgstabl", ell=ell, transpose=tr)
+        M = S.A.T if tr else S.A
+        rel = np.linalg.norm(b - M @ x) / np.linalg.norm(b)
+        assert rel <= 1e-8 * 1.01, (ell, tr, rel, st)
+        assert st[0]["matvecs"] >= 2 * ell
     A.close()

@@ -208,3 +208,23 @@ def test_native_csr_baseline_matches_oracle(oracle):
     xn, itn, rel = M.bicgstab(b, tol=1e-8, maxit=5000)
     assert rel < 1e-8 and abs(itn - ito) <= max(3, ito // 20), (itn, ito)
     assert np.linalg.norm(b - S.A @ xn) / np.linalg.norm(b) < 1e-7
+
+
+def test_native_bicgstabl_converges(oracle):
+    """The CPU baseline's BiCGStab(ℓ) reaches the tolerance on the same
+    system and, like the GPU solver, needs fewer operator applications than
+    BiCGSTAB there."""
+    from oracle.csr_native import NativeCSR
+    O = oracle
+    g = O.uniform_grid((12, 11, 10))
+    S = O.System(g, 2 * np.pi / 5.0, ((2, 2, 2), (2, 2, 2)), [O.Sphere((6.1, 5.2, 4.9), 2.6, 12.25)])
+    S.add_pointsrc((5.6, 5.5, 5.0), (0.2, 0.1, 1.0))
+    b = S.b()
+    M = NativeCSR(S.A, threads=2)
+    _, it, _ = M.bicgstab(b, tol=1e-8, maxit=20000)
+    for ell in (1, 2, 4):
+        x, mv, rel = M.bicgstabl(b, ell=ell, tol=1e-8, maxmv=40000)
+        assert rel < 1e-8, (ell, mv)
+        assert np.linalg.norm(b - S.A @ x) / np.linalg.norm(b) < 1e-7
+        if ell == 4:
+            assert mv <= 2 * it, (mv, it)
