@@ -45,29 +45,77 @@ __device__ __forceinline__ double2 scd(double2 a, double s) { return make_double
 template <typename R>
 __device__ __forceinline__ long long vstride() { return (long long)gridDim.x * VB; }
 
-// u_i = r_i − β u_i for i = 0 … j
-template <typename R>
-__global__ void __launch_bounds__(VB) k_bl_u(VSet<typename CT<R>::C> r, VSet<typename CT<R>::C> u, int j, long long n,
+// Two consecutive complex elements per access (16-byte loads for complex64).
+template <typename C> struct Pair { C a, b; };
+__device__ __forceinline__ Pair<float2> ldp(const float2 *__restrict__ p, long long q) {
+  const float4 v = reinterpret_cast<const float4 *>(p)[q];
+  return {make_float2(v.x, v.y), make_float2(v.z, v.w)};
+}
+__device__ __forceinline__ Pair<double2> ldp(const double2 *__restrict__ p, long long q) {
+  return {p[2 * q], p[2 * q + 1]};
+}
+__device__ __forceinline__ void stp(float2 *p, long long q, Pair<float2> v) {
+  reinterpret_cast<float4 *>(p)[q] = make_float4(v.a.x, v.a.y, v.b.x, v.b.y);
+}
+__device__ __forceinline__ void stp(double2 *p, long long q, Pair<double2> v) {
+  p[2 * q] = v.a;
+  p[2 * q + 1] = v.b;
+}
+
+// Grid-stride visit of element pairs (n is even: 3·Ncell with Ncell ≥ 2 …
+// an odd tail element is still handled, by block 0 thread 0).
+template <typename F2, typename F1>
+__device__ __forceinline__ void pairs(long long n, F2 f2, F1 f1) {
+  const long long np = n >> 1;
+  for (long long q = blockIdx.x * (long long)VB + threadIdx.x; q < np; q += (long long)gridDim.x * VB) f2(q);
+  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) f1(n - 1);
+}
+
+// u_i = r_i − β u_i for i = 0 … J
+template <typename R, int J>
+__global__ void __launch_bounds__(VB) k_bl_u(VSet<typename CT<R>::C> r, VSet<typename CT<R>::C> u, long long n,
                                              const KScalars *sc) {
   using C = typename CT<R>::C;
   if (sc->done) return;
   const C be = tocr<R>(sc->beta);
-  for (long long e = blockIdx.x * (long long)VB + threadIdx.x; e < n; e += vstride<R>()) {
-    for (int i = 0; i <= j; ++i) u.v[i][e] = csub(r.v[i][e], cmul(be, u.v[i][e]));
-  }
+  pairs(
+      n,
+      [&](long long q) {
+#pragma unroll
+        for (int i = 0; i <= J; ++i) {
+          const Pair<C> rv = ldp(r.v[i], q), uv = ldp(u.v[i], q);
+          stp(u.v[i], q, Pair<C>{csub(rv.a, cmul(be, uv.a)), csub(rv.b, cmul(be, uv.b))});
+        }
+      },
+      [&](long long e) {
+#pragma unroll
+        for (int i = 0; i <= J; ++i) u.v[i][e] = csub(r.v[i][e], cmul(be, u.v[i][e]));
+      });
 }
 
-// r_i −= α u_{i+1} for i = 0 … j;  x += α u_0
-template <typename R>
+// r_i −= α u_{i+1} for i = 0 … J;  x += α u_0
+template <typename R, int J>
 __global__ void __launch_bounds__(VB) k_bl_r(VSet<typename CT<R>::C> r, VSet<typename CT<R>::C> u,
-                                             typename CT<R>::C *x, int j, long long n, const KScalars *sc) {
+                                             typename CT<R>::C *x, long long n, const KScalars *sc) {
   using C = typename CT<R>::C;
   if (sc->done) return;
   const C al = tocr<R>(sc->alpha);
-  for (long long e = blockIdx.x * (long long)VB + threadIdx.x; e < n; e += vstride<R>()) {
-    for (int i = 0; i <= j; ++i) r.v[i][e] = csub(r.v[i][e], cmul(al, u.v[i + 1][e]));
-    x[e] = cadd(x[e], cmul(al, u.v[0][e]));
-  }
+  pairs(
+      n,
+      [&](long long q) {
+#pragma unroll
+        for (int i = 0; i <= J; ++i) {
+          const Pair<C> rv = ldp(r.v[i], q), uv = ldp(u.v[i + 1], q);
+          stp(r.v[i], q, Pair<C>{csub(rv.a, cmul(al, uv.a)), csub(rv.b, cmul(al, uv.b))});
+        }
+        const Pair<C> xv = ldp(x, q), u0 = ldp(u.v[0], q);
+        stp(x, q, Pair<C>{cadd(xv.a, cmul(al, u0.a)), cadd(xv.b, cmul(al, u0.b))});
+      },
+      [&](long long e) {
+#pragma unroll
+        for (int i = 0; i <= J; ++i) r.v[i][e] = csub(r.v[i][e], cmul(al, u.v[i + 1][e]));
+        x[e] = cadd(x[e], cmul(al, u.v[0][e]));
+      });
 }
 
 // Sum NV complex values over the block, write the block's partials, and
@@ -103,10 +151,30 @@ __device__ bool block_sums_last(double2 (&v)[NV], RedBuf red, double2 (&tot)[NV]
   __syncthreads();
   if (!last) return false;
   __threadfence();
+  // every thread sums a fixed subset of the blocks, then a fixed tree:
+  // deterministic for a given launch shape
+  double2 s[NV];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) s[q] = make_double2(0, 0);
+  for (unsigned b = tid; b < gridDim.x; b += VB)
+#pragma unroll
+    for (int q = 0; q < NV; ++q) s[q] = addd(s[q], __ldcg(&red.part[(long long)NV * b + q]));
+#pragma unroll
+  for (int q = 0; q < NV; ++q)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      s[q].x += __shfl_xor_sync(0xffffffffu, s[q].x, o);
+      s[q].y += __shfl_xor_sync(0xffffffffu, s[q].y, o);
+    }
+  __syncthreads();
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < NV; ++q) wred[wid][q] = s[q];
+  __syncthreads();
   if (tid < NV) {
-    double2 s = make_double2(0, 0);
-    for (unsigned b = 0; b < gridDim.x; ++b) s = addd(s, __ldcg(&red.part[(long long)NV * b + tid]));
-    tot[tid] = s;  // tot lives in shared memory of the caller
+    double2 t = make_double2(0, 0);
+    for (int w = 0; w < VB / 32; ++w) t = addd(t, wred[w][tid]);
+    tot[tid] = t;  // tot lives in shared memory of the caller
   }
   __syncthreads();
   if (tid == 0) *red.count = 0u;
@@ -123,10 +191,7 @@ __global__ void __launch_bounds__(VB) k_bl_gram(VSet<typename CT<R>::C> r, long 
   R ar[NV], ai[NV];
 #pragma unroll
   for (int q = 0; q < NV; ++q) ar[q] = ai[q] = R(0);
-  for (long long e = blockIdx.x * (long long)VB + threadIdx.x; e < n; e += vstride<R>()) {
-    C v[L + 1];
-#pragma unroll
-    for (int i = 0; i <= L; ++i) v[i] = r.v[i][e];
+  auto one = [&](const C (&v)[L + 1]) {
     int q = 0;
 #pragma unroll
     for (int j = 1; j <= L; ++j)
@@ -142,7 +207,26 @@ __global__ void __launch_bounds__(VB) k_bl_gram(VSet<typename CT<R>::C> r, long 
       ar[q] += d.x;
       ai[q] += d.y;
     }
-  }
+  };
+  pairs(
+      n,
+      [&](long long q) {
+        C va[L + 1], vb[L + 1];
+#pragma unroll
+        for (int i = 0; i <= L; ++i) {
+          const Pair<C> p = ldp(r.v[i], q);
+          va[i] = p.a;
+          vb[i] = p.b;
+        }
+        one(va);
+        one(vb);
+      },
+      [&](long long e) {
+        C v[L + 1];
+#pragma unroll
+        for (int i = 0; i <= L; ++i) v[i] = r.v[i][e];
+        one(v);
+      });
   double2 acc[NV];
 #pragma unroll
   for (int q = 0; q < NV; ++q) acc[q] = make_double2((double)ar[q], (double)ai[q]);
@@ -228,26 +312,58 @@ __global__ void __launch_bounds__(VB) k_bl_fin(VSet<typename CT<R>::C> r, VSet<t
     cu[k] = tocr<R>(sc->cu[k]);
   }
   Acc<R> a0r, a0i, a1;
-  for (long long e = blockIdx.x * (long long)VB + threadIdx.x; e < n; e += vstride<R>()) {
-    C rv[L + 1];
+  pairs(
+      n,
+      [&](long long q) {
+        C ra[L + 1], rb[L + 1], ua[L + 1], ub[L + 1];
 #pragma unroll
-    for (int k = 0; k <= L; ++k) rv[k] = r.v[k][e];
-    C xe = x[e], r0 = rv[0], u0 = u.v[0][e];
+        for (int k = 0; k <= L; ++k) {
+          const Pair<C> pr = ldp(r.v[k], q), pu = ldp(u.v[k], q);
+          ra[k] = pr.a;
+          rb[k] = pr.b;
+          ua[k] = pu.a;
+          ub[k] = pu.b;
+        }
+        Pair<C> xv = ldp(x, q);
+        const Pair<C> hv = ldp(rh, q);
+        C r0a = ra[0], r0b = rb[0], u0a = ua[0], u0b = ub[0];
 #pragma unroll
-    for (int k = 0; k <= L; ++k) xe = cadd(xe, cmul(cx[k], rv[k]));
+        for (int k = 0; k <= L; ++k) {
+          xv.a = cadd(xv.a, cmul(cx[k], ra[k]));
+          xv.b = cadd(xv.b, cmul(cx[k], rb[k]));
+        }
 #pragma unroll
-    for (int k = 1; k <= L; ++k) {
-      r0 = cadd(r0, cmul(cr[k], rv[k]));
-      u0 = cadd(u0, cmul(cu[k], u.v[k][e]));
-    }
-    x[e] = xe;
-    r.v[0][e] = r0;
-    u.v[0][e] = u0;
-    const C d = cdotc(rh[e], r0);
-    a0r.add(d.x);
-    a0i.add(d.y);
-    a1.add(r0.x * r0.x + r0.y * r0.y);
-  }
+        for (int k = 1; k <= L; ++k) {
+          r0a = cadd(r0a, cmul(cr[k], ra[k]));
+          r0b = cadd(r0b, cmul(cr[k], rb[k]));
+          u0a = cadd(u0a, cmul(cu[k], ua[k]));
+          u0b = cadd(u0b, cmul(cu[k], ub[k]));
+        }
+        stp(x, q, xv);
+        stp(r.v[0], q, Pair<C>{r0a, r0b});
+        stp(u.v[0], q, Pair<C>{u0a, u0b});
+        const C da = cdotc(hv.a, r0a), db = cdotc(hv.b, r0b);
+        a0r.add(da.x + db.x);
+        a0i.add(da.y + db.y);
+        a1.add((r0a.x * r0a.x + r0a.y * r0a.y) + (r0b.x * r0b.x + r0b.y * r0b.y));
+      },
+      [&](long long e) {
+        C xe = x[e], r0 = r.v[0][e], u0 = u.v[0][e];
+#pragma unroll
+        for (int k = 0; k <= L; ++k) xe = cadd(xe, cmul(cx[k], r.v[k][e]));
+#pragma unroll
+        for (int k = 1; k <= L; ++k) {
+          r0 = cadd(r0, cmul(cr[k], r.v[k][e]));
+          u0 = cadd(u0, cmul(cu[k], u.v[k][e]));
+        }
+        x[e] = xe;
+        r.v[0][e] = r0;
+        u.v[0][e] = u0;
+        const C d = cdotc(rh[e], r0);
+        a0r.add(d.x);
+        a0i.add(d.y);
+        a1.add(r0.x * r0.x + r0.y * r0.y);
+      });
   block_reduce_finalise<VB>(make_double2(a0r.get(), a0i.get()), make_double2(a1.get(), 0.0), red, FIN_BL_CYCLE, sc);
 }
 
@@ -281,11 +397,21 @@ static int bl_cycle_t(fdfd_handle *h, typename CT<R>::C *x, typename CT<R>::C *r
   const VSet<typename CT<R>::C> rs = vset<R>(r, L + 1), us = vset<R>(u, L + 1);
   int rc;
   for (int j = 0; j < L; ++j) {
-    k_bl_u<R><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, j, n, sc);
+    switch (j) {
+      case 0: k_bl_u<R, 0><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, n, sc); break;
+      case 1: k_bl_u<R, 1><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, n, sc); break;
+      case 2: k_bl_u<R, 2><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, n, sc); break;
+      default: k_bl_u<R, 3><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, n, sc); break;
+    }
     h->launches++;
     if ((rc = cuda_check(h, cudaGetLastError(), "k_bl_u"))) return rc;
     if ((rc = launch_apply_fin<R>(h, u[j], u[j + 1], EPI_DOT_AUX, rh, FIN_ALPHA, sc, tr))) return rc;
-    k_bl_r<R><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, j, n, sc);
+    switch (j) {
+      case 0: k_bl_r<R, 0><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
+      case 1: k_bl_r<R, 1><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
+      case 2: k_bl_r<R, 2><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
+      default: k_bl_r<R, 3><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
+    }
     h->launches++;
     if ((rc = cuda_check(h, cudaGetLastError(), "k_bl_r"))) return rc;
     if (j + 1 < L) rc = launch_apply_fin<R>(h, r[j], r[j + 1], EPI_DOT_AUX, rh, FIN_BL_RHO, sc, tr);
