@@ -118,21 +118,45 @@ __global__ void __launch_bounds__(VB) k_bl_r(VSet<typename CT<R>::C> r, VSet<typ
       });
 }
 
+// Error-free FP32 addition (Knuth's TwoSum): s + e == a + b exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// Warp sum of FP32 values carried as (hi, lo) pairs without rounding loss at
+// each level; returns the warp total as FP64 in lane 0's (hi + lo).  Avoids
+// FP64 arithmetic, whose pipe on this GPU is a small fraction of FP32.
+__device__ __forceinline__ double warp_sum_f32(float v) {
+  float hi = v, lo = 0.f;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, hi, o), ol = __shfl_xor_sync(0xffffffffu, lo, o);
+    float s, e;
+    two_sum(hi, oh, s, e);
+    hi = s;
+    lo = lo + ol + e;
+  }
+  return (double)hi + (double)lo;
+}
+
 // Sum NV complex values over the block, write the block's partials, and
 // return true in the block that arrives last (which then holds the grid
 // sums, in block order, in `tot`).
-template <int NV>
+template <int NV, bool WARP_DONE>
 __device__ bool block_sums_last(double2 (&v)[NV], RedBuf red, double2 (&tot)[NV]) {
   __shared__ double2 wred[VB / 32][NV];
   __shared__ bool last;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  if (!WARP_DONE)
 #pragma unroll
-  for (int q = 0; q < NV; ++q)
+    for (int q = 0; q < NV; ++q)
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      v[q].x += __shfl_xor_sync(0xffffffffu, v[q].x, o);
-      v[q].y += __shfl_xor_sync(0xffffffffu, v[q].y, o);
-    }
+      for (int o = 16; o > 0; o >>= 1) {
+        v[q].x += __shfl_xor_sync(0xffffffffu, v[q].x, o);
+        v[q].y += __shfl_xor_sync(0xffffffffu, v[q].y, o);
+      }
   if (lane == 0)
 #pragma unroll
     for (int q = 0; q < NV; ++q) wred[wid][q] = v[q];
@@ -184,7 +208,7 @@ __device__ bool block_sums_last(double2 (&v)[NV], RedBuf red, double2 (&tot)[NV]
 // Gram matrix of r_0 … r_L — (r_i, r_j) for 1 ≤ i ≤ j ≤ L, then (r_i, r_0)
 // for 1 ≤ i ≤ L — and, in the last block, the minimal-residual step.
 template <typename R, int L>
-__global__ void __launch_bounds__(VB) k_bl_gram(VSet<typename CT<R>::C> r, long long n, RedBuf red, KScalars *sc) {
+__global__ void __launch_bounds__(VB, 2) k_bl_gram(VSet<typename CT<R>::C> r, long long n, RedBuf red, KScalars *sc) {
   using C = typename CT<R>::C;
   constexpr int NV = L * (L + 1) / 2 + L;
   if (sc->done) return;
@@ -228,10 +252,16 @@ __global__ void __launch_bounds__(VB) k_bl_gram(VSet<typename CT<R>::C> r, long 
         one(v);
       });
   double2 acc[NV];
+  if constexpr (sizeof(R) == 4) {
+    // warp totals by FP32 two-sum trees; only lane 0's values matter below
 #pragma unroll
-  for (int q = 0; q < NV; ++q) acc[q] = make_double2((double)ar[q], (double)ai[q]);
+    for (int q = 0; q < NV; ++q) acc[q] = make_double2(warp_sum_f32(ar[q]), warp_sum_f32(ai[q]));
+  } else {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) acc[q] = make_double2((double)ar[q], (double)ai[q]);
+  }
   __shared__ double2 tot[NV];
-  if (!block_sums_last<NV>(acc, red, tot)) return;
+  if (!block_sums_last<NV, sizeof(R) == 4>(acc, red, tot)) return;
   if (threadIdx.x != 0) return;
   // Gram matrix G[i][j] = (r_i, r_j), i, j ≥ 1, and g0[i] = (r_i, r_0)
   double2 G[L + 1][L + 1], g0[L + 1];
@@ -299,7 +329,7 @@ __global__ void __launch_bounds__(VB) k_bl_gram(VSet<typename CT<R>::C> r, long 
 // x += Σ cx_k r_k ; r_0 += Σ cr_k r_k ; u_0 += Σ cu_k u_k ; then (r̂, r_0)
 // and ‖r_0‖² → FIN_BL_CYCLE
 template <typename R, int L>
-__global__ void __launch_bounds__(VB) k_bl_fin(VSet<typename CT<R>::C> r, VSet<typename CT<R>::C> u,
+__global__ void __launch_bounds__(VB, 3) k_bl_fin(VSet<typename CT<R>::C> r, VSet<typename CT<R>::C> u,
                                                typename CT<R>::C *x, const typename CT<R>::C *__restrict__ rh,
                                                long long n, RedBuf red, KScalars *sc) {
   using C = typename CT<R>::C;
