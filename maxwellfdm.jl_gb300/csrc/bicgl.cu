@@ -118,29 +118,6 @@ __global__ void __launch_bounds__(VB) k_bl_r(VSet<typename CT<R>::C> r, VSet<typ
       });
 }
 
-// Error-free FP32 addition (Knuth's TwoSum): s + e == a + b exactly.
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
-  s = a + b;
-  const float bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
-}
-
-// Warp sum of FP32 values carried as (hi, lo) pairs without rounding loss at
-// each level; returns the warp total as FP64 in lane 0's (hi + lo).  Avoids
-// FP64 arithmetic, whose pipe on this GPU is a small fraction of FP32.
-__device__ __forceinline__ double warp_sum_f32(float v) {
-  float hi = v, lo = 0.f;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const float oh = __shfl_xor_sync(0xffffffffu, hi, o), ol = __shfl_xor_sync(0xffffffffu, lo, o);
-    float s, e;
-    two_sum(hi, oh, s, e);
-    hi = s;
-    lo = lo + ol + e;
-  }
-  return (double)hi + (double)lo;
-}
-
 // Sum NV complex values over the block, write the block's partials, and
 // return true in the block that arrives last (which then holds the grid
 // sums, in block order, in `tot`).
@@ -255,7 +232,7 @@ __global__ void __launch_bounds__(VB, 2) k_bl_gram(VSet<typename CT<R>::C> r, lo
   if constexpr (sizeof(R) == 4) {
     // warp totals by FP32 two-sum trees; only lane 0's values matter below
 #pragma unroll
-    for (int q = 0; q < NV; ++q) acc[q] = make_double2(warp_sum_f32(ar[q]), warp_sum_f32(ai[q]));
+    for (int q = 0; q < NV; ++q) acc[q] = make_double2(warp_sum_split(ar[q]), warp_sum_split(ai[q]));
   } else {
 #pragma unroll
     for (int q = 0; q < NV; ++q) acc[q] = make_double2((double)ar[q], (double)ai[q]);
@@ -394,7 +371,7 @@ __global__ void __launch_bounds__(VB, 3) k_bl_fin(VSet<typename CT<R>::C> r, VSe
         a0i.add(d.y);
         a1.add(r0.x * r0.x + r0.y * r0.y);
       });
-  block_reduce_finalise<VB>(make_double2(a0r.get(), a0i.get()), make_double2(a1.get(), 0.0), red, FIN_BL_CYCLE, sc);
+  block_reduce_finalise<VB, sizeof(R) == 4>(make_double2(a0r.get(), a0i.get()), make_double2(a1.get(), 0.0), red, FIN_BL_CYCLE, sc);
 }
 
 // (r̂, r_0) for a replaced residual → FIN_BL_REDO
@@ -409,7 +386,7 @@ __global__ void __launch_bounds__(VB) k_bl_redo(const typename CT<R>::C *__restr
     a0r.add(d.x);
     a0i.add(d.y);
   }
-  block_reduce_finalise<VB>(make_double2(a0r.get(), a0i.get()), make_double2(0.0, 0.0), red, FIN_BL_REDO, sc);
+  block_reduce_finalise<VB, sizeof(R) == 4>(make_double2(a0r.get(), a0i.get()), make_double2(0.0, 0.0), red, FIN_BL_REDO, sc);
 }
 
 }  // namespace

@@ -103,18 +103,51 @@ __device__ inline void finalise(int mode, KScalars *sc, double2 d0, double2 d1) 
   }
 }
 
+// Error-free FP32 addition (Knuth's TwoSum): s + e == a + b exactly.
+__device__ __forceinline__ void two_sum_f(float a, float b, float &s, float &e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// Warp sum of a value that carries at most about 48 significant bits (an
+// FP32 sum, or a compensated FP32 sum widened to FP64): split into FP32
+// (hi, lo), add along an FP32 TwoSum tree, widen once.  The GPU's FP64 pipe
+// is a small fraction of its FP32 pipe, so the warp trees of the complex64
+// kernels avoid FP64 additions altogether.
+__device__ __forceinline__ double warp_sum_split(double x) {
+  float hi = (float)x, lo = (float)(x - (double)hi);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, hi, o), ol = __shfl_xor_sync(0xffffffffu, lo, o);
+    float s, e;
+    two_sum_f(hi, oh, s, e);
+    hi = s;
+    lo = lo + ol + e;
+  }
+  return (double)hi + (double)lo;
+}
+
 // Block-level reduction of two complex FP64 values, then the grid-level
 // last-block finalisation.  Must be called by every thread of the block.
-template <int NT>
+// F32 (complex64 kernels): the warp trees run in FP32 TwoSum arithmetic.
+template <int NT, bool F32 = false>
 __device__ inline void block_reduce_finalise(double2 a0, double2 a1, RedBuf red, int mode, KScalars *sc) {
   __shared__ double2 wred[NT / 32][2];
   __shared__ bool last;
+  if (F32) {
+    a0.x = warp_sum_split(a0.x);
+    a0.y = warp_sum_split(a0.y);
+    a1.x = warp_sum_split(a1.x);
+    a1.y = warp_sum_split(a1.y);
+  } else {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    a0.x += __shfl_xor_sync(0xffffffffu, a0.x, o);
-    a0.y += __shfl_xor_sync(0xffffffffu, a0.y, o);
-    a1.x += __shfl_xor_sync(0xffffffffu, a1.x, o);
-    a1.y += __shfl_xor_sync(0xffffffffu, a1.y, o);
+    for (int o = 16; o > 0; o >>= 1) {
+      a0.x += __shfl_xor_sync(0xffffffffu, a0.x, o);
+      a0.y += __shfl_xor_sync(0xffffffffu, a0.y, o);
+      a1.x += __shfl_xor_sync(0xffffffffu, a1.x, o);
+      a1.y += __shfl_xor_sync(0xffffffffu, a1.y, o);
+    }
   }
   const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
   const int lane = tid & 31, wid = tid >> 5;
