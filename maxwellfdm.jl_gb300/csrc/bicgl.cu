@@ -8,9 +8,11 @@
 // One cycle = 4ℓ + 2 kernels, all reading their scalars from device memory
 // (so a batch of cycles replays as one CUDA graph):
 //   for j = 0 … ℓ−1:
-//     u_i = r_i − β u_i (i ≤ j)                      k_bl_u
+//     u_i = r_i − β u_i (i ≤ j)                      k_bl_u (+ the deferred
+//                                                    updates of step j−1)
 //     u_{j+1} = A u_j, γ = (r̂, u_{j+1}), α = ρ/γ     operator, EPI_DOT_AUX + FIN_ALPHA
-//     r_i −= α u_{i+1} (i ≤ j), x += α u_0           k_bl_r
+//     r_j −= α u_{j+1}; the other r_i and x are      k_bl_r
+//     updated by the next k_bl_u (or here, last step)
 //     r_{j+1} = A r_j [, ρ₁ = (r̂, r_{j+1}), β]       operator, EPI_DOT_AUX + FIN_BL_RHO
 //   Gram matrix of r_0 … r_ℓ and the minimal-residual coefficients
 //   (modified Gram–Schmidt carried out on the Gram matrix)    k_bl_gram
@@ -71,50 +73,86 @@ __device__ __forceinline__ void pairs(long long n, F2 f2, F1 f1) {
   if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) f1(n - 1);
 }
 
-// u_i = r_i − β u_i for i = 0 … J
+// BiCG step J of a cycle, first half: u_i = r_i − β u_i for i = 0 … J.
+// For J ≥ 1 it first completes the previous step's updates that the
+// operator did not need (step J−1 updated only r_{J−1}):
+//   r_i −= α u_{i+1} (i < J−1) and x += α u_0, with α of step J−1 —
+// one pass over those vectors instead of two.
 template <typename R, int J>
-__global__ void __launch_bounds__(VB) k_bl_u(VSet<typename CT<R>::C> r, VSet<typename CT<R>::C> u, long long n,
-                                             const KScalars *sc) {
+__global__ void __launch_bounds__(VB) k_bl_u(VSet<typename CT<R>::C> r, VSet<typename CT<R>::C> u,
+                                             typename CT<R>::C *x, long long n, const KScalars *sc) {
   using C = typename CT<R>::C;
   if (sc->done) return;
-  const C be = tocr<R>(sc->beta);
+  const C be = tocr<R>(sc->beta), al = tocr<R>(sc->alpha);
   pairs(
       n,
       [&](long long q) {
+        Pair<C> rv[J + 1], uv[J + 1];
 #pragma unroll
         for (int i = 0; i <= J; ++i) {
-          const Pair<C> rv = ldp(r.v[i], q), uv = ldp(u.v[i], q);
-          stp(u.v[i], q, Pair<C>{csub(rv.a, cmul(be, uv.a)), csub(rv.b, cmul(be, uv.b))});
+          rv[i] = ldp(r.v[i], q);
+          uv[i] = ldp(u.v[i], q);
         }
+        if (J >= 1) {
+#pragma unroll
+          for (int i = 0; i + 1 < J; ++i) {
+            rv[i] = Pair<C>{csub(rv[i].a, cmul(al, uv[i + 1].a)), csub(rv[i].b, cmul(al, uv[i + 1].b))};
+            stp(r.v[i], q, rv[i]);
+          }
+          const Pair<C> xv = ldp(x, q);
+          stp(x, q, Pair<C>{cadd(xv.a, cmul(al, uv[0].a)), cadd(xv.b, cmul(al, uv[0].b))});
+        }
+#pragma unroll
+        for (int i = 0; i <= J; ++i)
+          stp(u.v[i], q, Pair<C>{csub(rv[i].a, cmul(be, uv[i].a)), csub(rv[i].b, cmul(be, uv[i].b))});
       },
       [&](long long e) {
+        C rv[J + 1], uv[J + 1];
 #pragma unroll
-        for (int i = 0; i <= J; ++i) u.v[i][e] = csub(r.v[i][e], cmul(be, u.v[i][e]));
+        for (int i = 0; i <= J; ++i) {
+          rv[i] = r.v[i][e];
+          uv[i] = u.v[i][e];
+        }
+        if (J >= 1) {
+#pragma unroll
+          for (int i = 0; i + 1 < J; ++i) {
+            rv[i] = csub(rv[i], cmul(al, uv[i + 1]));
+            r.v[i][e] = rv[i];
+          }
+          x[e] = cadd(x[e], cmul(al, uv[0]));
+        }
+#pragma unroll
+        for (int i = 0; i <= J; ++i) u.v[i][e] = csub(rv[i], cmul(be, uv[i]));
       });
 }
 
-// r_i −= α u_{i+1} for i = 0 … J;  x += α u_0
-template <typename R, int J>
+// BiCG step J, second half: r_J −= α u_{J+1} (the operator's next input);
+// FULL (the cycle's last step, before the Gram matrix): also r_i −= α u_{i+1}
+// for i < J and x += α u_0.
+template <typename R, int J, bool FULL>
 __global__ void __launch_bounds__(VB) k_bl_r(VSet<typename CT<R>::C> r, VSet<typename CT<R>::C> u,
                                              typename CT<R>::C *x, long long n, const KScalars *sc) {
   using C = typename CT<R>::C;
   if (sc->done) return;
   const C al = tocr<R>(sc->alpha);
+  constexpr int I0 = FULL ? 0 : J;
   pairs(
       n,
       [&](long long q) {
 #pragma unroll
-        for (int i = 0; i <= J; ++i) {
+        for (int i = I0; i <= J; ++i) {
           const Pair<C> rv = ldp(r.v[i], q), uv = ldp(u.v[i + 1], q);
           stp(r.v[i], q, Pair<C>{csub(rv.a, cmul(al, uv.a)), csub(rv.b, cmul(al, uv.b))});
         }
-        const Pair<C> xv = ldp(x, q), u0 = ldp(u.v[0], q);
-        stp(x, q, Pair<C>{cadd(xv.a, cmul(al, u0.a)), cadd(xv.b, cmul(al, u0.b))});
+        if (FULL) {
+          const Pair<C> xv = ldp(x, q), u0 = ldp(u.v[0], q);
+          stp(x, q, Pair<C>{cadd(xv.a, cmul(al, u0.a)), cadd(xv.b, cmul(al, u0.b))});
+        }
       },
       [&](long long e) {
 #pragma unroll
-        for (int i = 0; i <= J; ++i) r.v[i][e] = csub(r.v[i][e], cmul(al, u.v[i + 1][e]));
-        x[e] = cadd(x[e], cmul(al, u.v[0][e]));
+        for (int i = I0; i <= J; ++i) r.v[i][e] = csub(r.v[i][e], cmul(al, u.v[i + 1][e]));
+        if (FULL) x[e] = cadd(x[e], cmul(al, u.v[0][e]));
       });
 }
 
@@ -405,19 +443,23 @@ static int bl_cycle_t(fdfd_handle *h, typename CT<R>::C *x, typename CT<R>::C *r
   int rc;
   for (int j = 0; j < L; ++j) {
     switch (j) {
-      case 0: k_bl_u<R, 0><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, n, sc); break;
-      case 1: k_bl_u<R, 1><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, n, sc); break;
-      case 2: k_bl_u<R, 2><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, n, sc); break;
-      default: k_bl_u<R, 3><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, n, sc); break;
+      case 0: k_bl_u<R, 0><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
+      case 1: k_bl_u<R, 1><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
+      case 2: k_bl_u<R, 2><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
+      default: k_bl_u<R, 3><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
     }
     h->launches++;
     if ((rc = cuda_check(h, cudaGetLastError(), "k_bl_u"))) return rc;
     if ((rc = launch_apply_fin<R>(h, u[j], u[j + 1], EPI_DOT_AUX, rh, FIN_ALPHA, sc, tr))) return rc;
-    switch (j) {
-      case 0: k_bl_r<R, 0><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
-      case 1: k_bl_r<R, 1><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
-      case 2: k_bl_r<R, 2><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
-      default: k_bl_r<R, 3><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
+    const bool full = j + 1 == L;
+    switch (j * 2 + (full ? 1 : 0)) {
+      case 0: k_bl_r<R, 0, false><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
+      case 1: k_bl_r<R, 0, true><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
+      case 2: k_bl_r<R, 1, false><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
+      case 3: k_bl_r<R, 1, true><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
+      case 4: k_bl_r<R, 2, false><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
+      case 5: k_bl_r<R, 2, true><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
+      default: k_bl_r<R, 3, true><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
     }
     h->launches++;
     if ((rc = cuda_check(h, cudaGetLastError(), "k_bl_r"))) return rc;
