@@ -5,7 +5,7 @@
 // degree-ℓ one does not; it needs markedly fewer operator applications in
 // both precisions, for about 1.3× the vector traffic per application.
 //
-// One cycle = 4ℓ + 2 kernels, all reading their scalars from device memory
+// One cycle = 4ℓ + 3 kernels, all reading their scalars from device memory
 // (so a batch of cycles replays as one CUDA graph):
 //   for j = 0 … ℓ−1:
 //     u_i = r_i − β u_i (i ≤ j)                      k_bl_u (+ the deferred
@@ -14,8 +14,9 @@
 //     r_j −= α u_{j+1}; the other r_i and x are      k_bl_r
 //     updated by the next k_bl_u (or here, last step)
 //     r_{j+1} = A r_j [, ρ₁ = (r̂, r_{j+1}), β]       operator, EPI_DOT_AUX + FIN_BL_RHO
-//   Gram matrix of r_0 … r_ℓ and the minimal-residual coefficients
-//   (modified Gram–Schmidt carried out on the Gram matrix)    k_bl_gram
+//   Gram matrix of r_0 … r_ℓ                                  k_bl_gram
+//   minimal-residual coefficients (modified Gram–Schmidt
+//   carried out on the Gram matrix, one thread)               k_bl_mr
 //   x, r_0, u_0 closing update, (r̂, r_0), ‖r_0‖², stop tests  k_bl_fin + FIN_BL_CYCLE
 // Vectors and products are in the solve's inner precision; every sum
 // across threads and blocks is FP64, in a fixed order.
@@ -221,7 +222,7 @@ __device__ bool block_sums_last(double2 (&v)[NV], RedBuf red, double2 (&tot)[NV]
 }
 
 // Gram matrix of r_0 … r_L — (r_i, r_j) for 1 ≤ i ≤ j ≤ L, then (r_i, r_0)
-// for 1 ≤ i ≤ L — and, in the last block, the minimal-residual step.
+// for 1 ≤ i ≤ L — into sc->gram (last block).
 template <typename R, int L>
 __global__ void __launch_bounds__(VB, 2) k_bl_gram(VSet<typename CT<R>::C> r, long long n, RedBuf red, KScalars *sc) {
   using C = typename CT<R>::C;
@@ -277,34 +278,52 @@ __global__ void __launch_bounds__(VB, 2) k_bl_gram(VSet<typename CT<R>::C> r, lo
   }
   __shared__ double2 tot[NV];
   if (!block_sums_last<NV, sizeof(R) == 4>(acc, red, tot)) return;
-  if (threadIdx.x != 0) return;
-  // Gram matrix G[i][j] = (r_i, r_j), i, j ≥ 1, and g0[i] = (r_i, r_0)
+  if (threadIdx.x < NV) sc->gram[threadIdx.x] = tot[threadIdx.x];
+}
+
+// The minimal-residual step of the cycle from the Gram matrix (one thread;
+// its own launch so the arrays stay in registers): modified Gram–Schmidt on
+// r_1 … r_ℓ carried out on the Gram matrix — r̂_j = Σ_k Lc[j][k] r_k —
+// then the closing coefficients in terms of the original r_k.
+template <int L>
+__global__ void k_bl_mr(KScalars *sc) {
+  if (threadIdx.x != 0 || sc->done) return;
   double2 G[L + 1][L + 1], g0[L + 1];
   {
     int q = 0;
+#pragma unroll
     for (int j = 1; j <= L; ++j)
+#pragma unroll
       for (int i = 1; i <= j; ++i, ++q) {
-        G[i][j] = tot[q];
-        G[j][i] = conjd(tot[q]);
+        G[i][j] = sc->gram[q];
+        G[j][i] = conjd(sc->gram[q]);
       }
-    for (int i = 1; i <= L; ++i, ++q) g0[i] = tot[q];
+#pragma unroll
+    for (int i = 1; i <= L; ++i, ++q) g0[i] = sc->gram[q];
   }
-  // orthogonalised r̂_j = Σ_k Lc[j][k] r_k (k ≤ j); τ, σ, γ' as in MGS
   double2 Lc[L + 1][L + 1], tau[L + 1][L + 1], gp[L + 1], gam[L + 1], gpp[L + 1];
-  double sig[L + 1];
+  double isig[L + 1];
+#pragma unroll
   for (int a = 0; a <= L; ++a)
+#pragma unroll
     for (int b = 0; b <= L; ++b) Lc[a][b] = tau[a][b] = make_double2(0, 0);
+#pragma unroll
   for (int j = 1; j <= L; ++j) {
     Lc[j][j] = make_double2(1, 0);
+#pragma unroll
     for (int i = 1; i < j; ++i) {
       double2 d = make_double2(0, 0);  // (r̂_i, r_j)
+#pragma unroll
       for (int k = 1; k <= i; ++k) d = addd(d, dcmul(conjd(Lc[i][k]), G[k][j]));
-      tau[i][j] = scd(d, 1.0 / sig[i]);
+      tau[i][j] = scd(d, isig[i]);
+#pragma unroll
       for (int k = 1; k <= i; ++k) Lc[j][k] = subd(Lc[j][k], dcmul(tau[i][j], Lc[i][k]));
     }
-    double s = 0.0;  // (r̂_j, r̂_j)
+    double s = 0.0;                  // (r̂_j, r̂_j)
     double2 g = make_double2(0, 0);  // (r̂_j, r_0)
+#pragma unroll
     for (int k = 1; k <= j; ++k) {
+#pragma unroll
       for (int m = 1; m <= j; ++m) s += dcmul(dcmul(conjd(Lc[j][k]), Lc[j][m]), G[k][m]).x;
       g = addd(g, dcmul(conjd(Lc[j][k]), g0[k]));
     }
@@ -313,26 +332,33 @@ __global__ void __launch_bounds__(VB, 2) k_bl_gram(VSet<typename CT<R>::C> r, lo
       sc->reason = isfinite(s) ? 3 : 4;
       return;
     }
-    sig[j] = s;
-    gp[j] = scd(g, 1.0 / s);
+    isig[j] = 1.0 / s;
+    gp[j] = scd(g, isig[j]);
   }
   gam[L] = gp[L];
+#pragma unroll
   for (int j = L - 1; j >= 1; --j) {
     double2 t = gp[j];
+#pragma unroll
     for (int i = j + 1; i <= L; ++i) t = subd(t, dcmul(tau[j][i], gam[i]));
     gam[j] = t;
   }
+#pragma unroll
   for (int j = 1; j < L; ++j) {
     double2 t = gam[j + 1];
+#pragma unroll
     for (int i = j + 1; i < L; ++i) t = addd(t, dcmul(tau[j][i], gam[i + 1]));
     gpp[j] = t;
   }
-  // closing update in terms of the original r_k
+#pragma unroll
   for (int k = 0; k <= LMAX; ++k) sc->cx[k] = sc->cr[k] = sc->cu[k] = make_double2(0, 0);
   sc->cx[0] = gam[1];
+#pragma unroll
   for (int k = 1; k <= L; ++k) {
     double2 cx = make_double2(0, 0), cr = make_double2(0, 0);
+#pragma unroll
     for (int j = k; j < L; ++j) cx = addd(cx, dcmul(gpp[j], Lc[j][k]));
+#pragma unroll
     for (int j = k; j <= L; ++j) cr = subd(cr, dcmul(gp[j], Lc[j][k]));
     sc->cx[k] = cx;
     sc->cr[k] = cr;
@@ -471,6 +497,9 @@ static int bl_cycle_t(fdfd_handle *h, typename CT<R>::C *x, typename CT<R>::C *r
   k_bl_gram<R, L><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, n, h->red, sc);
   h->launches++;
   if ((rc = cuda_check(h, cudaGetLastError(), "k_bl_gram"))) return rc;
+  k_bl_mr<L><<<1, 32, 0, h->stream>>>(sc);
+  h->launches++;
+  if ((rc = cuda_check(h, cudaGetLastError(), "k_bl_mr"))) return rc;
   k_bl_fin<R, L><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, rh, n, h->red, sc);
   h->launches++;
   return cuda_check(h, cudaGetLastError(), "k_bl_fin");

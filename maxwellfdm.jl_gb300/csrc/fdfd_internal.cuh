@@ -93,6 +93,7 @@ struct KScalars {
   // the cycle's closing update x += Σ cx_k r_k, r₀ += Σ cr_k r_k, u₀ += Σ cu_k u_k
   double2 rho_pre;
   double2 cx[5], cr[5], cu[5];
+  double2 gram[14];  // (r_i, r_j), 1 ≤ i ≤ j ≤ ℓ, then (r_i, r_0)
 };
 
 struct Workspace;  // solver vectors (solver.cu)
