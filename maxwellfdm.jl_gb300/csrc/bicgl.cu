@@ -10,10 +10,12 @@
 //   for j = 0 … ℓ−1:
 //     u_i = r_i − β u_i (i ≤ j)                      k_bl_u (+ the deferred
 //                                                    updates of step j−1)
-//     u_{j+1} = A u_j, γ = (r̂, u_{j+1}), α = ρ/γ     operator, EPI_DOT_AUX + FIN_ALPHA
+//     u_{j+1} = A u_j, γ = (r̂, u_{j+1}), α = ρ/γ     operator, EPI_DOT_SHD + FIN_ALPHA
 //     r_j −= α u_{j+1}; the other r_i and x are      k_bl_r
 //     updated by the next k_bl_u (or here, last step)
-//     r_{j+1} = A r_j [, ρ₁ = (r̂, r_{j+1}), β]       operator, EPI_DOT_AUX + FIN_BL_RHO
+//     r_{j+1} = A r_j [, ρ₁ = (r̂, r_{j+1}), β]       operator, EPI_DOT_SHD + FIN_BL_RHO
+// r̂ is the generated shadow vector (shadow() in krylov_fin.cuh): no
+// memory traffic for it.
 //   Gram matrix of r_0 … r_ℓ                                  k_bl_gram
 //   minimal-residual coefficients (modified Gram–Schmidt
 //   carried out on the Gram matrix, one thread)               k_bl_mr
@@ -371,8 +373,7 @@ __global__ void k_bl_mr(KScalars *sc) {
 // and ‖r_0‖² → FIN_BL_CYCLE
 template <typename R, int L>
 __global__ void __launch_bounds__(VB, 3) k_bl_fin(VSet<typename CT<R>::C> r, VSet<typename CT<R>::C> u,
-                                               typename CT<R>::C *x, const typename CT<R>::C *__restrict__ rh,
-                                               long long n, RedBuf red, KScalars *sc) {
+                                                  typename CT<R>::C *x, long long n, RedBuf red, KScalars *sc) {
   using C = typename CT<R>::C;
   if (sc->done) return;
   C cx[L + 1], cr[L + 1], cu[L + 1];
@@ -396,7 +397,7 @@ __global__ void __launch_bounds__(VB, 3) k_bl_fin(VSet<typename CT<R>::C> r, VSe
           ub[k] = pu.b;
         }
         Pair<C> xv = ldp(x, q);
-        const Pair<C> hv = ldp(rh, q);
+        const Pair<C> hv{shadow<R>(2 * q), shadow<R>(2 * q + 1)};
         C r0a = ra[0], r0b = rb[0], u0a = ua[0], u0b = ub[0];
 #pragma unroll
         for (int k = 0; k <= L; ++k) {
@@ -430,7 +431,7 @@ __global__ void __launch_bounds__(VB, 3) k_bl_fin(VSet<typename CT<R>::C> r, VSe
         x[e] = xe;
         r.v[0][e] = r0;
         u.v[0][e] = u0;
-        const C d = cdotc(rh[e], r0);
+        const C d = cdotc(shadow<R>(e), r0);
         a0r.add(d.x);
         a0i.add(d.y);
         a1.add(r0.x * r0.x + r0.y * r0.y);
@@ -438,19 +439,19 @@ __global__ void __launch_bounds__(VB, 3) k_bl_fin(VSet<typename CT<R>::C> r, VSe
   block_reduce_finalise<VB, sizeof(R) == 4>(make_double2(a0r.get(), a0i.get()), make_double2(a1.get(), 0.0), red, FIN_BL_CYCLE, sc);
 }
 
-// (r̂, r_0) for a replaced residual → FIN_BL_REDO
+// (r̂, r_0) with the generated shadow vector: FIN_BL_REDO after a replaced
+// residual, FIN_NONE (into dot0) for the first ρ of a (re)started solve
 template <typename R>
-__global__ void __launch_bounds__(VB) k_bl_redo(const typename CT<R>::C *__restrict__ rh,
-                                                const typename CT<R>::C *__restrict__ r0, long long n, RedBuf red,
-                                                KScalars *sc) {
+__global__ void __launch_bounds__(VB) k_bl_redo(const typename CT<R>::C *__restrict__ r0, long long n, RedBuf red,
+                                                int fin, KScalars *sc) {
   using C = typename CT<R>::C;
   Acc<R> a0r, a0i;
   for (long long e = blockIdx.x * (long long)VB + threadIdx.x; e < n; e += vstride<R>()) {
-    const C d = cdotc(rh[e], r0[e]);
+    const C d = cdotc(shadow<R>(e), r0[e]);
     a0r.add(d.x);
     a0i.add(d.y);
   }
-  block_reduce_finalise<VB, sizeof(R) == 4>(make_double2(a0r.get(), a0i.get()), make_double2(0.0, 0.0), red, FIN_BL_REDO, sc);
+  block_reduce_finalise<VB, sizeof(R) == 4>(make_double2(a0r.get(), a0i.get()), make_double2(0.0, 0.0), red, fin, sc);
 }
 
 }  // namespace
@@ -463,8 +464,8 @@ static VSet<typename CT<R>::C> vset(typename CT<R>::C *const *v, int count) {
 }
 
 template <typename R, int L>
-static int bl_cycle_t(fdfd_handle *h, typename CT<R>::C *x, typename CT<R>::C *rh, typename CT<R>::C *const *r,
-                      typename CT<R>::C *const *u, long long n, KScalars *sc, bool tr) {
+static int bl_cycle_t(fdfd_handle *h, typename CT<R>::C *x, typename CT<R>::C *const *r, typename CT<R>::C *const *u,
+                      long long n, KScalars *sc, bool tr) {
   const VSet<typename CT<R>::C> rs = vset<R>(r, L + 1), us = vset<R>(u, L + 1);
   int rc;
   for (int j = 0; j < L; ++j) {
@@ -476,7 +477,7 @@ static int bl_cycle_t(fdfd_handle *h, typename CT<R>::C *x, typename CT<R>::C *r
     }
     h->launches++;
     if ((rc = cuda_check(h, cudaGetLastError(), "k_bl_u"))) return rc;
-    if ((rc = launch_apply_fin<R>(h, u[j], u[j + 1], EPI_DOT_AUX, rh, FIN_ALPHA, sc, tr))) return rc;
+    if ((rc = launch_apply_fin<R>(h, u[j], u[j + 1], EPI_DOT_SHD, nullptr, FIN_ALPHA, sc, tr))) return rc;
     const bool full = j + 1 == L;
     switch (j * 2 + (full ? 1 : 0)) {
       case 0: k_bl_r<R, 0, false><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
@@ -489,7 +490,7 @@ static int bl_cycle_t(fdfd_handle *h, typename CT<R>::C *x, typename CT<R>::C *r
     }
     h->launches++;
     if ((rc = cuda_check(h, cudaGetLastError(), "k_bl_r"))) return rc;
-    if (j + 1 < L) rc = launch_apply_fin<R>(h, r[j], r[j + 1], EPI_DOT_AUX, rh, FIN_BL_RHO, sc, tr);
+    if (j + 1 < L) rc = launch_apply_fin<R>(h, r[j], r[j + 1], EPI_DOT_SHD, nullptr, FIN_BL_RHO, sc, tr);
     else rc = launch_apply_fin<R>(h, r[j], r[j + 1], EPI_STORE, nullptr, FIN_NONE, sc, tr);
     if (rc) return rc;
   }
@@ -500,38 +501,38 @@ static int bl_cycle_t(fdfd_handle *h, typename CT<R>::C *x, typename CT<R>::C *r
   k_bl_mr<L><<<1, 32, 0, h->stream>>>(sc);
   h->launches++;
   if ((rc = cuda_check(h, cudaGetLastError(), "k_bl_mr"))) return rc;
-  k_bl_fin<R, L><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, rh, n, h->red, sc);
+  k_bl_fin<R, L><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, h->red, sc);
   h->launches++;
   return cuda_check(h, cudaGetLastError(), "k_bl_fin");
 }
 
 // One BiCGStab(ℓ) cycle (2ℓ operator applications).
 template <typename R>
-int bl_cycle(fdfd_handle *h, typename CT<R>::C *x, typename CT<R>::C *rh, typename CT<R>::C *const *r,
-             typename CT<R>::C *const *u, long long n, int ell, KScalars *sc, bool tr) {
+int bl_cycle(fdfd_handle *h, typename CT<R>::C *x, typename CT<R>::C *const *r, typename CT<R>::C *const *u,
+             long long n, int ell, KScalars *sc, bool tr) {
   switch (ell) {
-    case 1: return bl_cycle_t<R, 1>(h, x, rh, r, u, n, sc, tr);
-    case 2: return bl_cycle_t<R, 2>(h, x, rh, r, u, n, sc, tr);
-    case 3: return bl_cycle_t<R, 3>(h, x, rh, r, u, n, sc, tr);
-    case 4: return bl_cycle_t<R, 4>(h, x, rh, r, u, n, sc, tr);
+    case 1: return bl_cycle_t<R, 1>(h, x, r, u, n, sc, tr);
+    case 2: return bl_cycle_t<R, 2>(h, x, r, u, n, sc, tr);
+    case 3: return bl_cycle_t<R, 3>(h, x, r, u, n, sc, tr);
+    case 4: return bl_cycle_t<R, 4>(h, x, r, u, n, sc, tr);
   }
   return set_error(h, FDFD_ERR_ARG, "BiCGStab(l) needs 1 <= l <= 4");
 }
 
 template <typename R>
-int bl_redo(fdfd_handle *h, const typename CT<R>::C *rh, const typename CT<R>::C *r0, long long n, KScalars *sc) {
+int bl_redo(fdfd_handle *h, const typename CT<R>::C *r0, long long n, int fin, KScalars *sc) {
   int rc = ensure_red(h, RED_BLOCKS);
   if (rc) return rc;
-  k_bl_redo<R><<<RED_BLOCKS, VB, 0, h->stream>>>(rh, r0, n, h->red, sc);
+  k_bl_redo<R><<<RED_BLOCKS, VB, 0, h->stream>>>(r0, n, h->red, fin, sc);
   h->launches++;
   return cuda_check(h, cudaGetLastError(), "k_bl_redo");
 }
 
-template int bl_cycle<float>(fdfd_handle *, float2 *, float2 *, float2 *const *, float2 *const *, long long, int,
-                             KScalars *, bool);
-template int bl_cycle<double>(fdfd_handle *, double2 *, double2 *, double2 *const *, double2 *const *, long long,
-                              int, KScalars *, bool);
-template int bl_redo<float>(fdfd_handle *, const float2 *, const float2 *, long long, KScalars *);
-template int bl_redo<double>(fdfd_handle *, const double2 *, const double2 *, long long, KScalars *);
+template int bl_cycle<float>(fdfd_handle *, float2 *, float2 *const *, float2 *const *, long long, int, KScalars *,
+                             bool);
+template int bl_cycle<double>(fdfd_handle *, double2 *, double2 *const *, double2 *const *, long long, int,
+                              KScalars *, bool);
+template int bl_redo<float>(fdfd_handle *, const float2 *, long long, int, KScalars *);
+template int bl_redo<double>(fdfd_handle *, const double2 *, long long, int, KScalars *);
 
 }  // namespace fdfd

@@ -67,6 +67,7 @@ enum EpiKind : int {
   EPI_DOT_AUX = 2,      // y = A x, accumulate conj(aux0)·y     (aux0 = r̂)
   EPI_DOT_TS = 3,       // y = A x, accumulate conj(y)·x, ‖y‖²  (t = A s)
   EPI_DOT_SU = 4,       // y = A x, accumulate Σ V_E·x·y (unconjugated, COCG's pᵀ S q)
+  EPI_DOT_SHD = 5,      // y = A x, accumulate conj(r̂)·y with the generated shadow vector r̂
 };
 
 // Reduction slots used by the fused kernels: each kernel accumulates up to

@@ -174,6 +174,11 @@ __global__ void __launch_bounds__(NTHR, 2) k_apply_hh(OpArgs<R> a, Extra<R> ex, 
         const C d0 = cdotc(aux0[3 * cell], yx), d1 = cdotc(aux0[3 * cell + 1], yy), d2 = cdotc(aux0[3 * cell + 2], yz);
         r0.add(d0.x + d1.x + d2.x);
         i0acc.add(d0.y + d1.y + d2.y);
+      } else if (EPI == EPI_DOT_SHD) {
+        const C d0 = cdotc(shadow<R>(3 * cell), yx), d1 = cdotc(shadow<R>(3 * cell + 1), yy),
+                d2 = cdotc(shadow<R>(3 * cell + 2), yz);
+        r0.add(d0.x + d1.x + d2.x);
+        i0acc.add(d0.y + d1.y + d2.y);
       } else if (EPI == EPI_DOT_TS) {
         const C d0 = cdotc(yx, hx), d1 = cdotc(yy, hy), d2 = cdotc(yz, hz);
         r0.add(d0.x + d1.x + d2.x);
@@ -225,6 +230,7 @@ int launch_apply_hh(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R>::
     case EPI_RESID: return launch_hh_t<R, EPI_RESID>(h, x, y, aux0, fin, sc);
     case EPI_DOT_AUX: return launch_hh_t<R, EPI_DOT_AUX>(h, x, y, aux0, fin, sc);
     case EPI_DOT_TS: return launch_hh_t<R, EPI_DOT_TS>(h, x, y, aux0, fin, sc);
+    case EPI_DOT_SHD: return launch_hh_t<R, EPI_DOT_SHD>(h, x, y, aux0, fin, sc);
   }
   return set_error(h, FDFD_ERR_UNSUPPORTED, "this reduction is not available for the H formulation");
 }

@@ -103,6 +103,29 @@ __device__ inline void finalise(int mode, KScalars *sc, double2 d0, double2 d1) 
   }
 }
 
+// The BiCGStab(ℓ) shadow vector r̂, generated from the DOF index instead of
+// stored: r̂_i = (a + i·b)/32768 with a, b the two 16-bit halves (as signed
+// integers) of a 32-bit integer hash of i — Chris Wellons' "lowbias32"
+// mixing function (xor-shift / multiply rounds).  Any fixed r̂ is a valid
+// shadow vector; a random one converged at least as fast as r̂ = r₀ on
+// these systems, and generating it saves a vector read in every operator
+// application with a dot product.  The values are exact in FP32, so both
+// precisions use the same r̂.
+__host__ __device__ __forceinline__ uint32_t shadow_hash(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352dU;
+  x ^= x >> 15;
+  x *= 0x846ca68bU;
+  x ^= x >> 16;
+  return x;
+}
+template <typename R>
+__device__ __forceinline__ typename CT<R>::C shadow(long long dof) {
+  const uint32_t hsh = shadow_hash((uint32_t)dof);
+  const int re = (int)(int16_t)(hsh & 0xffffu), im = (int)(int16_t)(hsh >> 16);
+  return mk(R(re) * R(1.0 / 32768.0), R(im) * R(1.0 / 32768.0));
+}
+
 // Error-free FP32 addition (Knuth's TwoSum): s + e == a + b exactly.
 __device__ __forceinline__ void two_sum_f(float a, float b, float &s, float &e) {
   s = a + b;

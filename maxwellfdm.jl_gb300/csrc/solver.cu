@@ -52,10 +52,10 @@ int demote(fdfd_handle *, float2 *, const double2 *, long long);
 int promote(fdfd_handle *, double2 *, const float2 *, long long);
 int build_weights(fdfd_handle *h, double2 *w64, float2 *w32, double2 *d64, float2 *d32);
 template <typename R>
-int bl_cycle(fdfd_handle *, typename CT<R>::C *, typename CT<R>::C *, typename CT<R>::C *const *,
-             typename CT<R>::C *const *, long long, int, KScalars *, bool);
+int bl_cycle(fdfd_handle *, typename CT<R>::C *, typename CT<R>::C *const *, typename CT<R>::C *const *, long long,
+             int, KScalars *, bool);
 template <typename R>
-int bl_redo(fdfd_handle *, const typename CT<R>::C *, const typename CT<R>::C *, long long, KScalars *);
+int bl_redo(fdfd_handle *, const typename CT<R>::C *, long long, int, KScalars *);
 
 #define TRY(x)              \
   do {                      \
@@ -224,8 +224,8 @@ static int cocg_iter(fdfd_handle *h, Workspace *ws, bool tr) {
   return FDFD_OK;
 }
 
-// One BiCGStab(ℓ) cycle.  Vectors: 0 x (correction), 1 r̂, 2 … 2+ℓ r_0 … r_ℓ,
-// 3+ℓ … 3+2ℓ u_0 … u_ℓ.
+// One BiCGStab(ℓ) cycle.  Vectors: 0 x (correction), 2 … 2+ℓ r_0 … r_ℓ,
+// 3+ℓ … 3+2ℓ u_0 … u_ℓ (slot 1 unused: r̂ is generated).
 template <typename R>
 static int bl_iter(fdfd_handle *h, Workspace *ws, int ell, bool tr) {
   using C = typename CT<R>::C;
@@ -234,7 +234,7 @@ static int bl_iter(fdfd_handle *h, Workspace *ws, int ell, bool tr) {
     r[i] = vec<R>(ws, 2 + i);
     u[i] = vec<R>(ws, 3 + ell + i);
   }
-  return bl_cycle<R>(h, vec<R>(ws, 0), vec<R>(ws, 1), r, u, ws->n, ell, ws->sc, tr);
+  return bl_cycle<R>(h, vec<R>(ws, 0), r, u, ws->n, ell, ws->sc, tr);
 }
 
 // ρ = rᵀ S D⁻¹ r of the current residual (q is used as scratch for D⁻¹ r)
@@ -298,14 +298,17 @@ static int init_inner(fdfd_handle *h, Workspace *ws, int method, int ell, double
   const long long n = ws->n;
   const size_t bytes = (size_t)n * sizeof(C);
   if (method == FDFD_BICGSTABL) {
-    // r_0 = r64, r̂ = r_0, u_0 = 0, x = 0; ρ₀ = (r̂, r_0), α = 0 so the first β is 0
+    // r_0 = r64, u_0 = 0, x = 0; ρ₀ = (r̂, r_0) with the generated shadow
+    // vector r̂; α = 0 so the first β is 0
     C *r0 = vec<R>(ws, 2);
     if constexpr (sizeof(R) == 4) TRY(demote(h, r0, ws->r64, n));
     else TRY(copy<double>(h, r0, ws->r64, n));
-    TRY(copy<R>(h, vec<R>(ws, 1), r0, n));
     TRY(cuda_check(h, cudaMemsetAsync(vec<R>(ws, 0), 0, bytes, h->stream), "memset x"));
     TRY(cuda_check(h, cudaMemsetAsync(vec<R>(ws, 3 + ell), 0, bytes, h->stream), "memset u0"));
-    hs->rho = make_double2(rr, 0.0);
+    TRY(bl_redo<R>(h, r0, n, FIN_NONE, ws->scu));
+    KScalars tmp;
+    TRY(read_scalars(h, ws->scu, &tmp));
+    hs->rho = tmp.dot0;
     hs->alpha = make_double2(0.0, 0.0);
     hs->omega = make_double2(1.0, 0.0);
     hs->beta = make_double2(0.0, 0.0);
@@ -421,7 +424,7 @@ static int solve_impl(fdfd_handle *h, const double2 *b, double2 *x, const fdfd_s
           } else if (o.method == FDFD_BICGSTABL) {
             // ρ₁ = (r̂, r_0) and β of the next cycle for the replaced r_0
             TRY(write_scalars(h, ws->sc, &hs));
-            TRY(bl_redo<R>(h, vec<R>(ws, 1), r, n, ws->sc));
+            TRY(bl_redo<R>(h, r, n, FIN_BL_REDO, ws->sc));
             TRY(read_scalars(h, ws->sc, &hs));
           }
         }

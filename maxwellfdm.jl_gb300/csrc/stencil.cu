@@ -413,6 +413,11 @@ __device__ __forceinline__ void output_cell(const HTile<R> &H, const CoefTile<R>
     acc.r0.add(d0.x + d1.x + d2.x);
     acc.i0.add(d0.y + d1.y + d2.y);
     acc.r1.add(yx.x * yx.x + yx.y * yx.y + yy.x * yy.x + yy.y * yy.y + yz.x * yz.x + yz.y * yz.y);
+  } else if (EPI == EPI_DOT_SHD) {
+    const C d0 = cdotc(shadow<R>(3 * cell), yx), d1 = cdotc(shadow<R>(3 * cell + 1), yy),
+            d2 = cdotc(shadow<R>(3 * cell + 2), yz);
+    acc.r0.add(d0.x + d1.x + d2.x);
+    acc.i0.add(d0.y + d1.y + d2.y);
   } else if (EPI == EPI_DOT_SU) {
     // Σ V_E·x·y over the cell (COCG's S-weighted bilinear form)
     const C d0 = cmul(cmul(vol_e<R>(ex, 0, gi, gj, k), e_x), yx);
@@ -1031,6 +1036,7 @@ int launch_apply_fin(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R>:
       case EPI_RESID: return launch_t<R, EPI_RESID, true>(h, x, y, aux0, fin, sc);
       case EPI_DOT_AUX: return launch_t<R, EPI_DOT_AUX, true>(h, x, y, aux0, fin, sc);
       case EPI_DOT_TS: return launch_t<R, EPI_DOT_TS, true>(h, x, y, aux0, fin, sc);
+      case EPI_DOT_SHD: return launch_t<R, EPI_DOT_SHD, true>(h, x, y, aux0, fin, sc);
     }
   } else {
     switch (epi) {
@@ -1039,6 +1045,7 @@ int launch_apply_fin(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R>:
       case EPI_DOT_AUX: return launch_t<R, EPI_DOT_AUX, false>(h, x, y, aux0, fin, sc);
       case EPI_DOT_TS: return launch_t<R, EPI_DOT_TS, false>(h, x, y, aux0, fin, sc);
       case EPI_DOT_SU: return launch_t<R, EPI_DOT_SU, false>(h, x, y, aux0, fin, sc);
+      case EPI_DOT_SHD: return launch_t<R, EPI_DOT_SHD, false>(h, x, y, aux0, fin, sc);
     }
   }
   return set_error(h, FDFD_ERR_ARG, "bad epilogue kind");

@@ -154,10 +154,21 @@ static void xpay(int64_t n, const cplx *x, cplx a, cplx *y) { /* y = x + a y */
 static inline cplx csub_(cplx a, cplx b) { cplx r = {a.re - b.re, a.im - b.im}; return r; }
 static inline cplx cadd_(cplx a, cplx b) { cplx r = {a.re + b.re, a.im + b.im}; return r; }
 
+/* Shadow vector of the GPU solver: r̂_i = (a + i b)/32768 with a, b the two
+ * 16-bit halves (signed) of Chris Wellons' "lowbias32" hash of i. */
+static uint32_t shadow_hash(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352dU;
+  x ^= x >> 15;
+  x *= 0x846ca68bU;
+  x ^= x >> 16;
+  return x;
+}
+
 /* BiCGStab(l), l <= 8, with the modified Gram-Schmidt minimal-residual part
- * of the original algorithm; same stopping rule as csr_bicgstab (recursive
- * residual).  Returns the operator applications done (-1 on allocation
- * failure). */
+ * of the original algorithm and the GPU solver's generated shadow vector;
+ * same stopping rule as csr_bicgstab (recursive residual).  Returns the
+ * operator applications done (-1 on allocation failure). */
 int64_t csr_bicgstabl(int64_t n, const int64_t *indptr, const int32_t *indices, const double *data, const double *b,
                       double *x, int l, double tol, int64_t maxmv, double *relres) {
   enum { LM = 8 };
@@ -178,7 +189,9 @@ int64_t csr_bicgstabl(int64_t n, const int64_t *indptr, const int32_t *indices, 
     for (int64_t i = 0; i < n; ++i) {
       r[0][i].re = B[i].re - r[0][i].re;
       r[0][i].im = B[i].im - r[0][i].im;
-      rh[i] = r[0][i];
+      const uint32_t hsh = shadow_hash((uint32_t)i);
+      rh[i].re = (double)(int16_t)(hsh & 0xffffu) / 32768.0;
+      rh[i].im = (double)(int16_t)(hsh >> 16) / 32768.0;
     }
     const double nb = nrm2(n, B);
     cplx rho0 = {1, 0}, alpha = {0, 0}, om = {1, 0};

@@ -77,6 +77,6 @@ def test_no_device_reports_status(lib, pkg):
 
 def test_default_opts(lib, pkg):
     o = pkg._lib.default_opts()
-    assert o.method == pkg._lib.FDFD_BICGSTAB and o.precision == pkg._lib.FDFD_PREC_MIXED
+    assert o.method == pkg._lib.FDFD_BICGSTABL and o.ell == 4 and o.precision == pkg._lib.FDFD_PREC_MIXED
     assert o.tol == 1e-6 and o.delta == 0.1 and o.use_graph == 1
     assert lib.fdfd_version().startswith(b"fdfd_gb300")
