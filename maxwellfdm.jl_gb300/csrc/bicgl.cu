@@ -309,25 +309,30 @@ __global__ void k_bl_mr(KScalars *sc) {
   for (int a = 0; a <= L; ++a)
 #pragma unroll
     for (int b = 0; b <= L; ++b) Lc[a][b] = tau[a][b] = make_double2(0, 0);
+  double2 gr0[L + 1];  // (r̂_i, r_0)
 #pragma unroll
   for (int j = 1; j <= L; ++j) {
     Lc[j][j] = make_double2(1, 0);
+    double2 dij[L + 1];  // (r̂_i, r_j)
 #pragma unroll
     for (int i = 1; i < j; ++i) {
-      double2 d = make_double2(0, 0);  // (r̂_i, r_j)
+      double2 d = make_double2(0, 0);
 #pragma unroll
       for (int k = 1; k <= i; ++k) d = addd(d, dcmul(conjd(Lc[i][k]), G[k][j]));
+      dij[i] = d;
       tau[i][j] = scd(d, isig[i]);
 #pragma unroll
       for (int k = 1; k <= i; ++k) Lc[j][k] = subd(Lc[j][k], dcmul(tau[i][j], Lc[i][k]));
     }
-    double s = 0.0;                  // (r̂_j, r̂_j)
-    double2 g = make_double2(0, 0);  // (r̂_j, r_0)
+    // with r̂_j = r_j − Σ_{i<j} τ_ij r̂_i and the r̂_i orthogonal:
+    //   (r̂_j, r̂_j) = (r_j, r_j) − Σ_i |(r̂_i, r_j)|²/σ_i
+    //   (r̂_j, r_0)  = (r_j, r_0) − Σ_i conj(τ_ij) (r̂_i, r_0)
+    double s = G[j][j].x;
+    double2 g = g0[j];
 #pragma unroll
-    for (int k = 1; k <= j; ++k) {
-#pragma unroll
-      for (int m = 1; m <= j; ++m) s += dcmul(dcmul(conjd(Lc[j][k]), Lc[j][m]), G[k][m]).x;
-      g = addd(g, dcmul(conjd(Lc[j][k]), g0[k]));
+    for (int i = 1; i < j; ++i) {
+      s -= (dij[i].x * dij[i].x + dij[i].y * dij[i].y) * isig[i];
+      g = subd(g, dcmul(conjd(tau[i][j]), gr0[i]));
     }
     if (!(s > 0.0) || !isfinite(s)) {
       sc->done = 1;
@@ -335,6 +340,7 @@ __global__ void k_bl_mr(KScalars *sc) {
       return;
     }
     isig[j] = 1.0 / s;
+    gr0[j] = g;
     gp[j] = scd(g, isig[j]);
   }
   gam[L] = gp[L];
