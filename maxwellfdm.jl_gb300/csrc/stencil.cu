@@ -709,7 +709,7 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2)
     // only E(k), H and the staged corners, and the next iteration's first
     // barrier orders this plane's reads of H/corners before they are rewritten
     if (tid == 0) {
-      const int q = k + 3;
+      const int q = k + G::NSLOT - 1;  // the plane this freed slot takes
       if (q <= k1) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         issue_plane<R>(smraw, bars, &tmap, &emap, a, ex, tilecol, cx, cy, i0, j0, k0, q, sm);
