@@ -36,7 +36,7 @@ extern "C" {
 enum {
   FDFD_OK = 0,
   FDFD_ERR_ARG = 1,           /* invalid argument: NULL pointer, bad size or enum   */
-  FDFD_ERR_UNSUPPORTED = 2,   /* valid model feature this build does not implement  */
+  FDFD_ERR_UNSUPPORTED = 2,   /* valid model feature this library does not implement */
   FDFD_ERR_CUDA = 3,          /* CUDA runtime error                                  */
   FDFD_ERR_NOMEM = 4,         /* device or pinned-host allocation failed             */
   FDFD_ERR_NOT_CONVERGED = 5, /* solver reached maxit before tol                      */
@@ -74,7 +74,7 @@ enum { FDFD_SLICE_NONE = 0, FDFD_SLICE_TE = 1, FDFD_SLICE_TM = 2 };
 typedef struct {
   int32_t N[3];             /* cells per axis                                          */
   int32_t isbloch[3];       /* 1 = Bloch, 0 = symmetry boundary (PEC for boundft EE)   */
-  int32_t boundft[3];       /* FDFD_EE on every axis in this build                     */
+  int32_t boundft[3];       /* FDFD_EE on every axis (HH staggering: unsupported)   */
   int32_t order_cmpfirst;   /* must be 1                                               */
   int32_t device;           /* CUDA device ordinal                                     */
   int32_t slice2d;          /* FDFD_SLICE_NONE (3D), FDFD_SLICE_TE or FDFD_SLICE_TM      */
@@ -138,7 +138,7 @@ int fdfd_sync(fdfd_handle *h);
 /* ---- material ------------------------------------------------------------
  * Pε of create_paramops (model.jl:154-171).  εarr is the reference's
  * (Nx,Ny,Nz,3,3) column-major ComplexF64 array: diagonal entries at the E_w
- * samples, off-diagonal entries at E-voxel corners.  This build requires a
+ * samples, off-diagonal entries at E-voxel corners.  This library requires a
  * real, symmetric tensor (lossless dielectric); other input returns
  * FDFD_ERR_UNSUPPORTED. */
 int fdfd_set_eps_tensor(fdfd_handle *h, const double *epsarr);

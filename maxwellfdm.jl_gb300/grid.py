@@ -25,7 +25,7 @@ class Grid:
 
     def __init__(self, lprim, isbloch=(False, False, False)):
         if len(lprim) != 3:
-            raise ValueError("this build models 3D grids (ModelFull)")
+            raise ValueError("grids are 3D here (2D models use ModelTE/ModelTM)")
         self.lprim = tuple(np.array(l, dtype=np.float64) for l in lprim)
         for l in self.lprim:
             if l.ndim != 1 or len(l) < 2 or np.any(np.diff(l) <= 0):
