@@ -200,6 +200,13 @@ int fdfd_residual_dev_noalloc(fdfd_handle *h, const void *x, const void *b, void
  * other (each 2·3·Ncell doubles).  stats may be NULL or an array of nrhs. */
 int fdfd_solve(fdfd_handle *h, const double *b, double *x, int32_t nrhs,
                const fdfd_solve_opts *opts, fdfd_stats *stats);
+/* As fdfd_solve, with up to nworkers right-hand sides solved at the same
+ * time, each on its own CUDA stream and host thread (workers share the
+ * handle's operator data and own their Krylov workspace): small grids, whose
+ * kernels fill a fraction of the GPU, overlap.  Independent of the
+ * reference (which solves right-hand sides one by one). */
+int fdfd_solve_batch(fdfd_handle *h, const double *b, double *x, int32_t nrhs, int32_t nworkers,
+                     const fdfd_solve_opts *opts, fdfd_stats *stats);
 /* Device buffers (double2, 3·Ncell each) on the handle's stream; returns
  * after the solve completes. */
 int fdfd_solve_dev(fdfd_handle *h, const void *b, void *x,

@@ -79,6 +79,8 @@ SIGNATURES = {
     "fdfd_matvec_transpose": (C.c_int, [C.c_void_p, _dp, _dp, C.c_int32]),
     "fdfd_solve": (C.c_int, [C.c_void_p, _dp, _dp, C.c_int32, C.POINTER(fdfd_solve_opts),
                              C.POINTER(fdfd_stats)]),
+    "fdfd_solve_batch": (C.c_int, [C.c_void_p, _dp, _dp, C.c_int32, C.c_int32, C.POINTER(fdfd_solve_opts),
+                                   C.POINTER(fdfd_stats)]),
     "fdfd_solve_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(fdfd_solve_opts),
                                  C.POINTER(fdfd_stats)]),
     "fdfd_default_opts": (None, [C.POINTER(fdfd_solve_opts)]),

@@ -13,6 +13,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "krylov_fin.cuh"
@@ -441,14 +442,16 @@ void fdfd_destroy(fdfd_handle *h) {
   cudaSetDevice(h->dev);
   if (h->stream) cudaStreamSynchronize(h->stream);
   free_workspace(h);
-  cudaFree(h->coef64);
-  cudaFree(h->coef32);
-  cudaFree(h->eps64);
-  cudaFree(h->eps32);
-  cudaFree(h->eoff64);
-  cudaFree(h->eoff32);
-  cudaFree(h->oflag);
-  cudaFree(h->smask);
+  if (!h->shares_operator) {
+    cudaFree(h->coef64);
+    cudaFree(h->coef32);
+    cudaFree(h->eps64);
+    cudaFree(h->eps32);
+    cudaFree(h->eoff64);
+    cudaFree(h->eoff32);
+    cudaFree(h->oflag);
+    cudaFree(h->smask);
+  }
   cudaFree(h->vx64);
   cudaFree(h->vy64);
   cudaFree(h->ve64);
@@ -647,6 +650,109 @@ int fdfd_solve(fdfd_handle *h, const double *b, double *x, int32_t nrhs, const f
     if ((rc2 = cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync"))) return rc2;
   }
   if (first_err) return set_error(h, first_err, first_msg);
+  return FDFD_OK;
+}
+
+// A worker for concurrent solves: the parent's operator data (read-only
+// during a solve) with its own stream, events, reduction buffer, scalars,
+// workspace and scratch.
+static fdfd_handle *make_worker(fdfd_handle *p, int *rc) {
+  fdfd_handle *w = new fdfd_handle();
+  w->dev = p->dev;
+  for (int a = 0; a < 3; ++a) {
+    w->N[a] = p->N[a];
+    w->bloch[a] = p->bloch[a];
+    w->coef_off[a] = p->coef_off[a];
+    w->rlo[a] = p->rlo[a];
+    w->rhi[a] = p->rhi[a];
+    w->e_ikl[a][0] = p->e_ikl[a][0];
+    w->e_ikl[a][1] = p->e_ikl[a][1];
+  }
+  w->ncell = p->ncell;
+  w->omega[0] = p->omega[0];
+  w->omega[1] = p->omega[1];
+  w->w2[0] = p->w2[0];
+  w->w2[1] = p->w2[1];
+  w->coef64 = p->coef64;
+  w->coef32 = p->coef32;
+  w->coef_stride = p->coef_stride;
+  w->eps64 = p->eps64;
+  w->eps32 = p->eps32;
+  w->eoff64 = p->eoff64;
+  w->eoff32 = p->eoff32;
+  w->oflag = p->oflag;
+  w->has_off = p->has_off;
+  w->smask = p->smask;
+  w->slice2d = p->slice2d;
+  w->ft = p->ft;
+  w->tma_disabled = p->tma_disabled;
+  w->pdl = p->pdl;
+  w->kc[0] = p->kc[0];
+  w->kc[1] = p->kc[1];
+  w->kc_force = p->kc_force;
+  w->tuned_off = p->tuned_off;
+  w->shares_operator = true;
+  *rc = FDFD_OK;
+  if (cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&w->ev0) != cudaSuccess || cudaEventCreate(&w->ev1) != cudaSuccess ||
+      cudaMalloc(&w->util_sc, sizeof(KScalars)) != cudaSuccess || cudaMalloc(&w->dev_err, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    *rc = set_error(p, FDFD_ERR_NOMEM, "creating a batch worker failed");
+    return w;
+  }
+  cudaMemsetAsync(w->util_sc, 0, sizeof(KScalars), w->stream);
+  cudaMemsetAsync(w->dev_err, 0, sizeof(int), w->stream);
+  if ((*rc = ensure_red(w, apply_blocks(w)))) set_error(p, *rc, w->err);
+  return w;
+}
+
+int fdfd_solve_batch(fdfd_handle *h, const double *b, double *x, int32_t nrhs, int32_t nworkers,
+                     const fdfd_solve_opts *opts, fdfd_stats *stats) {
+  if (!h || !b || !x || nrhs < 1 || nworkers < 1) return set_error(h, FDFD_ERR_ARG, "bad argument");
+  int rc = check_opts(h, opts);
+  if (rc) return rc;
+  if (nworkers > nrhs) nworkers = nrhs;
+  if (nworkers == 1) return fdfd_solve(h, b, x, nrhs, opts, stats);
+  cudaSetDevice(h->dev);
+  if ((rc = cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync"))) return rc;
+  std::vector<fdfd_handle *> ws(nworkers, nullptr);
+  for (int t = 0; t < nworkers && rc == FDFD_OK; ++t) ws[t] = make_worker(h, &rc);
+  const int mask = field_mask(h, h->ft == FDFD_HH);
+  const long long n = __builtin_popcount(mask) * h->ncell;
+  std::vector<int> rcs(nworkers, FDFD_OK);
+  std::vector<std::string> msgs(nworkers);
+  if (rc == FDFD_OK) {
+    std::vector<std::thread> th;
+    for (int t = 0; t < nworkers; ++t) {
+      th.emplace_back([&, t]() {
+        fdfd_handle *w = ws[t];
+        cudaSetDevice(w->dev);
+        int r = ensure_scratch(w, false);
+        for (int q = t; q < nrhs && r == FDFD_OK; q += nworkers) {
+          if ((r = h2d_field(w, b + 2 * n * q, w->vx64, mask))) break;
+          if (opts->x0_given && (r = h2d_field(w, x + 2 * n * q, w->vy64, mask))) break;
+          int rs = solve_dev_impl(w, w->vx64, w->vy64, opts, stats ? stats + q : nullptr);
+          if (rs && rs != FDFD_ERR_NOT_CONVERGED && rs != FDFD_ERR_BREAKDOWN) { r = rs; break; }
+          if ((r = d2h_field(w, w->vy64, x + 2 * n * q, mask))) break;
+          if ((r = cuda_check(w, cudaStreamSynchronize(w->stream), "stream sync"))) break;
+          if (rs && rcs[t] == FDFD_OK) {
+            rcs[t] = rs;
+            msgs[t] = w->err;
+          }
+        }
+        if (r) {
+          rcs[t] = r;
+          msgs[t] = w->err;
+        }
+      });
+    }
+    for (auto &t : th) t.join();
+  }
+  for (auto *w : ws)
+    if (w) fdfd_destroy(w);
+  if (rc) return rc;
+  for (int t = 0; t < nworkers; ++t)
+    if (rcs[t]) return set_error(h, rcs[t], msgs[t]);
   return FDFD_OK;
 }
 

@@ -131,6 +131,7 @@ struct fdfd_handle {
   double2 *stage64 = nullptr;  // 2D slices: compact host-layout staging
   int slice2d = 0;             // FDFD_SLICE_NONE / _TE / _TM
   int ft = 0;                  // field solved for: FDFD_EE (A = CₘCₑ − ω²Pε) or FDFD_HH (A = CₑPε⁻¹Cₘ − ω²)
+  bool shares_operator = false;  // a batch worker: coefficients, ε and flags belong to its parent
   float2 *vx32 = nullptr, *vy32 = nullptr;
   fdfd::RedBuf red{nullptr, nullptr};
   int red_blocks = 0;

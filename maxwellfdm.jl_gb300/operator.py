@@ -175,10 +175,12 @@ class FDFDOperator:
 
     # ---------------------------------------------------------------- solve
     def solve(self, b, tol=1e-6, precision="mixed", method="bicgstabl", maxit=200000, x0=None, delta=0.1,
-              check_every=50, transpose=False, use_graph=True, ell=4):
+              check_every=50, transpose=False, use_graph=True, ell=4, workers=1):
         """x = A \\ b to a true relative residual ``tol``.  b may hold several
-        right-hand sides as rows of a 2D array.  method: "bicgstab", "bicgstabl"
-        (BiCGStab(ℓ), ℓ = ell) or "cocg".  Returns (x, [stats])."""
+        right-hand sides as rows of a 2D array; ``workers`` > 1 solves up to
+        that many of them at the same time on separate streams.  method:
+        "bicgstab", "bicgstabl" (BiCGStab(ℓ), ℓ = ell) or "cocg".  Returns
+        (x, [stats])."""
         b = np.ascontiguousarray(b, dtype=np.complex128)
         nrhs = 1 if b.ndim == 1 else b.shape[0]
         b2 = b.reshape(nrhs, -1)
@@ -187,7 +189,10 @@ class FDFDOperator:
         x = np.zeros_like(b2) if x0 is None else np.ascontiguousarray(x0, np.complex128).reshape(nrhs, -1).copy()
         o = self._opts(tol, precision, method, maxit, x0 is not None, delta, check_every, transpose, use_graph, ell)
         st = (_lib.fdfd_stats * nrhs)()
-        rc = self._lib.fdfd_solve(self._h, dptr(b2), dptr(x), nrhs, C.byref(o), st)
+        if workers > 1 and nrhs > 1:
+            rc = self._lib.fdfd_solve_batch(self._h, dptr(b2), dptr(x), nrhs, int(workers), C.byref(o), st)
+        else:
+            rc = self._lib.fdfd_solve(self._h, dptr(b2), dptr(x), nrhs, C.byref(o), st)
         stats = [s.as_dict() for s in st]
         if rc != _lib.FDFD_OK:
             err = _lib.FDFDError(rc, (self._lib.fdfd_last_error(self._h) or b"").decode())

@@ -117,3 +117,20 @@ def test_320_capped_solve_residual(big):
     rr = A.residual_dev(xd.data_ptr(), bd.data_ptr(), r.data_ptr())
     rel = rr ** 0.5 / np.linalg.norm(b)
     assert 0 < rel < 1.0
+
+
+def test_batch_of_rhs_on_concurrent_streams(pkg, oracle):
+    """All right-hand sides of one 48³ instance at once, one worker stream
+    each: the same answers as the one-by-one solve."""
+    wl = pkg.workloads
+    mdl, om, rhs = wl.config3_instance(C3_48[0])
+    A = pkg.create_A(mdl, om)
+    B = np.stack([wl.dipole_rhs(mdl, om, c, p) for c, p in rhs])
+    xs, sts = A.solve(B, tol=1e-7, precision="mixed")
+    xb, stb = A.solve(B, tol=1e-7, precision="mixed", workers=len(rhs))
+    for q in range(len(rhs)):
+        assert stb[q]["status"] == 0 and stb[q]["relres"] <= 1e-7, stb[q]
+        rel = np.linalg.norm(B[q] - A.matvec(xb[q])) / np.linalg.norm(B[q])
+        assert rel <= 1.01e-7, (q, rel)
+        assert np.linalg.norm(xb[q] - xs[q]) / np.linalg.norm(xs[q]) < 1e-5
+    A.close()
