@@ -12,7 +12,8 @@
 //                                                    updates of step j−1)
 //     u_{j+1} = A u_j, γ = (r̂, u_{j+1}), α = ρ/γ     operator, EPI_DOT_SHD + FIN_ALPHA
 //     r_j −= α u_{j+1}; the other r_i and x are      k_bl_r
-//     updated by the next k_bl_u (or here, last step)
+//     updated by the next k_bl_u (last step: by
+//     k_bl_gram and k_bl_fin, on the fly)
 //     r_{j+1} = A r_j [, ρ₁ = (r̂, r_{j+1}), β]       operator, EPI_DOT_SHD + FIN_BL_RHO
 // r̂ is the generated shadow vector (shadow() in krylov_fin.cuh): no
 // memory traffic for it.
@@ -20,8 +21,17 @@
 //   minimal-residual coefficients (modified Gram–Schmidt
 //   carried out on the Gram matrix, one thread)               k_bl_mr
 //   x, r_0, u_0 closing update, (r̂, r_0), ‖r_0‖², stop tests  k_bl_fin + FIN_BL_CYCLE
+// The last BiCG step's updates r_i −= α u_{i+1} (i < ℓ−1) and x += α u_0
+// are never stored: k_bl_gram and k_bl_fin read r_i and u_{i+1} anyway and
+// apply them in registers (only r_0, u_0 and x outlive the cycle), which
+// saves nine vector passes per cycle.
 // Vectors and products are in the solve's inner precision; every sum
 // across threads and blocks is FP64, in a fixed order.
+// The grid-stride vector kernels run one full wave (SM count × the
+// kernel's resident blocks per SM), so none ends on a partial wave.
+#include <mutex>
+#include <unordered_map>
+
 #include "krylov_fin.cuh"
 
 namespace fdfd {
@@ -129,52 +139,39 @@ __global__ void __launch_bounds__(VB) k_bl_u(VSet<typename CT<R>::C> r, VSet<typ
       });
 }
 
-// BiCG step J, second half: r_J −= α u_{J+1} (the operator's next input);
-// FULL (the cycle's last step, before the Gram matrix): also r_i −= α u_{i+1}
-// for i < J and x += α u_0.
-template <typename R, int J, bool FULL>
-__global__ void __launch_bounds__(VB) k_bl_r(VSet<typename CT<R>::C> r, VSet<typename CT<R>::C> u,
-                                             typename CT<R>::C *x, long long n, const KScalars *sc) {
+// BiCG step J, second half: r_J −= α u_{J+1} (the operator's next input).
+template <typename R, int J>
+__global__ void __launch_bounds__(VB) k_bl_r(VSet<typename CT<R>::C> r, VSet<typename CT<R>::C> u, long long n,
+                                             const KScalars *sc) {
   using C = typename CT<R>::C;
   if (sc->done) return;
   const C al = tocr<R>(sc->alpha);
-  constexpr int I0 = FULL ? 0 : J;
   pairs(
       n,
       [&](long long q) {
-#pragma unroll
-        for (int i = I0; i <= J; ++i) {
-          const Pair<C> rv = ldp(r.v[i], q), uv = ldp(u.v[i + 1], q);
-          stp(r.v[i], q, Pair<C>{csub(rv.a, cmul(al, uv.a)), csub(rv.b, cmul(al, uv.b))});
-        }
-        if (FULL) {
-          const Pair<C> xv = ldp(x, q), u0 = ldp(u.v[0], q);
-          stp(x, q, Pair<C>{cadd(xv.a, cmul(al, u0.a)), cadd(xv.b, cmul(al, u0.b))});
-        }
+        const Pair<C> rv = ldp(r.v[J], q), uv = ldp(u.v[J + 1], q);
+        stp(r.v[J], q, Pair<C>{csub(rv.a, cmul(al, uv.a)), csub(rv.b, cmul(al, uv.b))});
       },
-      [&](long long e) {
-#pragma unroll
-        for (int i = I0; i <= J; ++i) r.v[i][e] = csub(r.v[i][e], cmul(al, u.v[i + 1][e]));
-        if (FULL) x[e] = cadd(x[e], cmul(al, u.v[0][e]));
-      });
+      [&](long long e) { r.v[J][e] = csub(r.v[J][e], cmul(al, u.v[J + 1][e])); });
 }
 
-// Sum NV complex values over the block, write the block's partials, and
-// return true in the block that arrives last (which then holds the grid
-// sums, in block order, in `tot`).
-template <int NV, bool WARP_DONE>
+constexpr int pow2_at_least(int k) { return k <= 1 ? 1 : 2 * pow2_at_least((k + 1) / 2); }
+
+// Sum NV complex FP64 values over the block (complex128 kernels), write the
+// block's partials, and return true in the block that arrives last (which
+// then holds the grid sums, in block order, in `tot`).
+template <int NV>
 __device__ bool block_sums_last(double2 (&v)[NV], RedBuf red, double2 (&tot)[NV]) {
   __shared__ double2 wred[VB / 32][NV];
   __shared__ bool last;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  if (!WARP_DONE)
 #pragma unroll
-    for (int q = 0; q < NV; ++q)
+  for (int q = 0; q < NV; ++q)
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        v[q].x += __shfl_xor_sync(0xffffffffu, v[q].x, o);
-        v[q].y += __shfl_xor_sync(0xffffffffu, v[q].y, o);
-      }
+    for (int o = 16; o > 0; o >>= 1) {
+      v[q].x += __shfl_xor_sync(0xffffffffu, v[q].x, o);
+      v[q].y += __shfl_xor_sync(0xffffffffu, v[q].y, o);
+    }
   if (lane == 0)
 #pragma unroll
     for (int q = 0; q < NV; ++q) wred[wid][q] = v[q];
@@ -224,12 +221,16 @@ __device__ bool block_sums_last(double2 (&v)[NV], RedBuf red, double2 (&tot)[NV]
 }
 
 // Gram matrix of r_0 … r_L — (r_i, r_j) for 1 ≤ i ≤ j ≤ L, then (r_i, r_0)
-// for 1 ≤ i ≤ L — into sc->gram (last block).
+// for 1 ≤ i ≤ L — into sc->gram (last block).  The stored r_i (i < L−1)
+// still lack the last BiCG step's −α u_{i+1}; it is applied in registers.
 template <typename R, int L>
-__global__ void __launch_bounds__(VB, 2) k_bl_gram(VSet<typename CT<R>::C> r, long long n, RedBuf red, KScalars *sc) {
+__global__ void __launch_bounds__(VB, 2) k_bl_gram(VSet<typename CT<R>::C> r, VSet<typename CT<R>::C> u, long long n,
+                                                   RedBuf red, KScalars *sc) {
   using C = typename CT<R>::C;
   constexpr int NV = L * (L + 1) / 2 + L;
+  constexpr int ND = L > 1 ? L - 1 : 1;  // deferred corrections (L − 1 of them)
   if (sc->done) return;
+  const C al = tocr<R>(sc->alpha);
   R ar[NV], ai[NV];
 #pragma unroll
   for (int q = 0; q < NV; ++q) ar[q] = ai[q] = R(0);
@@ -254,11 +255,19 @@ __global__ void __launch_bounds__(VB, 2) k_bl_gram(VSet<typename CT<R>::C> r, lo
       n,
       [&](long long q) {
         C va[L + 1], vb[L + 1];
+        Pair<C> ud[ND];
 #pragma unroll
         for (int i = 0; i <= L; ++i) {
           const Pair<C> p = ldp(r.v[i], q);
           va[i] = p.a;
           vb[i] = p.b;
+        }
+#pragma unroll
+        for (int i = 0; i + 1 < L; ++i) ud[i] = ldp(u.v[i + 1], q);
+#pragma unroll
+        for (int i = 0; i + 1 < L; ++i) {
+          va[i] = csub(va[i], cmul(al, ud[i].a));
+          vb[i] = csub(vb[i], cmul(al, ud[i].b));
         }
         one(va);
         one(vb);
@@ -267,20 +276,31 @@ __global__ void __launch_bounds__(VB, 2) k_bl_gram(VSet<typename CT<R>::C> r, lo
         C v[L + 1];
 #pragma unroll
         for (int i = 0; i <= L; ++i) v[i] = r.v[i][e];
+#pragma unroll
+        for (int i = 0; i + 1 < L; ++i) v[i] = csub(v[i], cmul(al, u.v[i + 1][e]));
         one(v);
       });
-  double2 acc[NV];
   if constexpr (sizeof(R) == 4) {
-    // warp totals by FP32 two-sum trees; only lane 0's values matter below
+    constexpr int K = pow2_at_least(2 * NV);
+    DF v[K];
 #pragma unroll
-    for (int q = 0; q < NV; ++q) acc[q] = make_double2(warp_sum_split(ar[q]), warp_sum_split(ai[q]));
+    for (int q = 0; q < K; ++q) v[q] = DF{0.f, 0.f};
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+      v[2 * q].hi = ar[q];
+      v[2 * q + 1].hi = ai[q];
+    }
+    __shared__ double tot[2 * NV];
+    if (!df_block_sums_last<VB, K, 2 * NV>(v, red, tot)) return;
+    if (threadIdx.x < NV) sc->gram[threadIdx.x] = make_double2(tot[2 * threadIdx.x], tot[2 * threadIdx.x + 1]);
   } else {
+    double2 acc[NV];
 #pragma unroll
     for (int q = 0; q < NV; ++q) acc[q] = make_double2((double)ar[q], (double)ai[q]);
+    __shared__ double2 tot[NV];
+    if (!block_sums_last<NV>(acc, red, tot)) return;
+    if (threadIdx.x < NV) sc->gram[threadIdx.x] = tot[threadIdx.x];
   }
-  __shared__ double2 tot[NV];
-  if (!block_sums_last<NV, sizeof(R) == 4>(acc, red, tot)) return;
-  if (threadIdx.x < NV) sc->gram[threadIdx.x] = tot[threadIdx.x];
 }
 
 // The minimal-residual step of the cycle from the Gram matrix (one thread;
@@ -375,14 +395,17 @@ __global__ void k_bl_mr(KScalars *sc) {
   sc->omega = gam[L];
 }
 
-// x += Σ cx_k r_k ; r_0 += Σ cr_k r_k ; u_0 += Σ cu_k u_k ; then (r̂, r_0)
-// and ‖r_0‖² → FIN_BL_CYCLE
+// x += α u_0 + Σ cx_k r_k ; r_0 += Σ cr_k r_k ; u_0 += Σ cu_k u_k ; then
+// (r̂, r_0) and ‖r_0‖² → FIN_BL_CYCLE.  α u_0 and the r_i −= α u_{i+1}
+// (i < L−1) are the last BiCG step's deferred updates (α of that step:
+// nothing writes sc->alpha between it and this kernel).
 template <typename R, int L>
-__global__ void __launch_bounds__(VB, 3) k_bl_fin(VSet<typename CT<R>::C> r, VSet<typename CT<R>::C> u,
+__global__ void __launch_bounds__(VB, sizeof(R) == 4 ? 3 : 2) k_bl_fin(VSet<typename CT<R>::C> r, VSet<typename CT<R>::C> u,
                                                   typename CT<R>::C *x, long long n, RedBuf red, KScalars *sc) {
   using C = typename CT<R>::C;
   if (sc->done) return;
   C cx[L + 1], cr[L + 1], cu[L + 1];
+  const C al = tocr<R>(sc->alpha);
 #pragma unroll
   for (int k = 0; k <= L; ++k) {
     cx[k] = tocr<R>(sc->cx[k]);
@@ -404,6 +427,13 @@ __global__ void __launch_bounds__(VB, 3) k_bl_fin(VSet<typename CT<R>::C> r, VSe
         }
         Pair<C> xv = ldp(x, q);
         const Pair<C> hv{shadow<R>(2 * q), shadow<R>(2 * q + 1)};
+#pragma unroll
+        for (int k = 0; k + 1 < L; ++k) {
+          ra[k] = csub(ra[k], cmul(al, ua[k + 1]));
+          rb[k] = csub(rb[k], cmul(al, ub[k + 1]));
+        }
+        xv.a = cadd(xv.a, cmul(al, ua[0]));
+        xv.b = cadd(xv.b, cmul(al, ub[0]));
         C r0a = ra[0], r0b = rb[0], u0a = ua[0], u0b = ub[0];
 #pragma unroll
         for (int k = 0; k <= L; ++k) {
@@ -426,13 +456,21 @@ __global__ void __launch_bounds__(VB, 3) k_bl_fin(VSet<typename CT<R>::C> r, VSe
         a1.add((r0a.x * r0a.x + r0a.y * r0a.y) + (r0b.x * r0b.x + r0b.y * r0b.y));
       },
       [&](long long e) {
-        C xe = x[e], r0 = r.v[0][e], u0 = u.v[0][e];
+        C rk[L + 1], uk[L + 1];
 #pragma unroll
-        for (int k = 0; k <= L; ++k) xe = cadd(xe, cmul(cx[k], r.v[k][e]));
+        for (int k = 0; k <= L; ++k) {
+          rk[k] = r.v[k][e];
+          uk[k] = u.v[k][e];
+        }
+#pragma unroll
+        for (int k = 0; k + 1 < L; ++k) rk[k] = csub(rk[k], cmul(al, uk[k + 1]));
+        C xe = cadd(x[e], cmul(al, uk[0])), r0 = rk[0], u0 = uk[0];
+#pragma unroll
+        for (int k = 0; k <= L; ++k) xe = cadd(xe, cmul(cx[k], rk[k]));
 #pragma unroll
         for (int k = 1; k <= L; ++k) {
-          r0 = cadd(r0, cmul(cr[k], r.v[k][e]));
-          u0 = cadd(u0, cmul(cu[k], u.v[k][e]));
+          r0 = cadd(r0, cmul(cr[k], rk[k]));
+          u0 = cadd(u0, cmul(cu[k], uk[k]));
         }
         x[e] = xe;
         r.v[0][e] = r0;
@@ -442,7 +480,7 @@ __global__ void __launch_bounds__(VB, 3) k_bl_fin(VSet<typename CT<R>::C> r, VSe
         a0i.add(d.y);
         a1.add(r0.x * r0.x + r0.y * r0.y);
       });
-  block_reduce_finalise<VB, sizeof(R) == 4>(make_double2(a0r.get(), a0i.get()), make_double2(a1.get(), 0.0), red, FIN_BL_CYCLE, sc);
+  sum_finalise<VB>(a0r, a0i, a1, red, FIN_BL_CYCLE, sc);
 }
 
 // (r̂, r_0) with the generated shadow vector: FIN_BL_REDO after a replaced
@@ -457,7 +495,7 @@ __global__ void __launch_bounds__(VB) k_bl_redo(const typename CT<R>::C *__restr
     a0r.add(d.x);
     a0i.add(d.y);
   }
-  block_reduce_finalise<VB, sizeof(R) == 4>(make_double2(a0r.get(), a0i.get()), make_double2(0.0, 0.0), red, fin, sc);
+  sum_finalise<VB>(a0r, a0i, red, fin, sc);
 }
 
 }  // namespace
@@ -469,46 +507,66 @@ static VSet<typename CT<R>::C> vset(typename CT<R>::C *const *v, int count) {
   return s;
 }
 
+// Blocks for one full wave of a grid-stride kernel: SM count × its resident
+// blocks per SM (cached per kernel), at most `cap`.
+static int wave_blocks(const void *kern, int cap) {
+  static std::mutex mu;
+  static std::unordered_map<const void *, int> cache;
+  std::lock_guard<std::mutex> lock(mu);
+  const auto it = cache.find(kern);
+  if (it != cache.end()) return std::min(it->second, cap);
+  int dev = 0, sms = 0, per = 0;
+  int b = RED_BLOCKS;
+  if (cudaGetDevice(&dev) == cudaSuccess &&
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, VB, 0) == cudaSuccess && sms * per > 0)
+    b = sms * per;
+  cache.emplace(kern, b);
+  return std::min(b, cap);
+}
+
+// Launch a grid-stride vector kernel on one full wave.
+template <typename... P, typename... A>
+static void launch_wave(fdfd_handle *h, void (*kern)(P...), int cap, A... args) {
+  kern<<<wave_blocks(reinterpret_cast<const void *>(kern), cap), VB, 0, h->stream>>>(args...);
+  h->launches++;
+}
+
 template <typename R, int L>
 static int bl_cycle_t(fdfd_handle *h, typename CT<R>::C *x, typename CT<R>::C *const *r, typename CT<R>::C *const *u,
                       long long n, KScalars *sc, bool tr) {
   const VSet<typename CT<R>::C> rs = vset<R>(r, L + 1), us = vset<R>(u, L + 1);
+  constexpr int NOCAP = 1 << 30;
   int rc;
   for (int j = 0; j < L; ++j) {
     switch (j) {
-      case 0: k_bl_u<R, 0><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
-      case 1: k_bl_u<R, 1><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
-      case 2: k_bl_u<R, 2><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
-      default: k_bl_u<R, 3><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
+      case 0: launch_wave(h, k_bl_u<R, 0>, NOCAP, rs, us, x, n, (const KScalars *)sc); break;
+      case 1: launch_wave(h, k_bl_u<R, 1>, NOCAP, rs, us, x, n, (const KScalars *)sc); break;
+      case 2: launch_wave(h, k_bl_u<R, 2>, NOCAP, rs, us, x, n, (const KScalars *)sc); break;
+      default: launch_wave(h, k_bl_u<R, 3>, NOCAP, rs, us, x, n, (const KScalars *)sc); break;
     }
-    h->launches++;
     if ((rc = cuda_check(h, cudaGetLastError(), "k_bl_u"))) return rc;
     if ((rc = launch_apply_fin<R>(h, u[j], u[j + 1], EPI_DOT_SHD, nullptr, FIN_ALPHA, sc, tr))) return rc;
-    const bool full = j + 1 == L;
-    switch (j * 2 + (full ? 1 : 0)) {
-      case 0: k_bl_r<R, 0, false><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
-      case 1: k_bl_r<R, 0, true><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
-      case 2: k_bl_r<R, 1, false><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
-      case 3: k_bl_r<R, 1, true><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
-      case 4: k_bl_r<R, 2, false><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
-      case 5: k_bl_r<R, 2, true><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
-      default: k_bl_r<R, 3, true><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, sc); break;
+    switch (j) {
+      case 0: launch_wave(h, k_bl_r<R, 0>, NOCAP, rs, us, n, (const KScalars *)sc); break;
+      case 1: launch_wave(h, k_bl_r<R, 1>, NOCAP, rs, us, n, (const KScalars *)sc); break;
+      case 2: launch_wave(h, k_bl_r<R, 2>, NOCAP, rs, us, n, (const KScalars *)sc); break;
+      default: launch_wave(h, k_bl_r<R, 3>, NOCAP, rs, us, n, (const KScalars *)sc); break;
     }
-    h->launches++;
     if ((rc = cuda_check(h, cudaGetLastError(), "k_bl_r"))) return rc;
     if (j + 1 < L) rc = launch_apply_fin<R>(h, r[j], r[j + 1], EPI_DOT_SHD, nullptr, FIN_BL_RHO, sc, tr);
     else rc = launch_apply_fin<R>(h, r[j], r[j + 1], EPI_STORE, nullptr, FIN_NONE, sc, tr);
     if (rc) return rc;
   }
+  // the reducing kernels keep ≤ RED_BLOCKS blocks: 8·RED_BLOCKS partial
+  // slots hold the Gram matrix's L(L+1)/2 + L ≤ 14 values per block
   if ((rc = ensure_red(h, 8 * RED_BLOCKS))) return rc;
-  k_bl_gram<R, L><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, n, h->red, sc);
-  h->launches++;
+  launch_wave(h, k_bl_gram<R, L>, RED_BLOCKS, rs, us, n, h->red, sc);
   if ((rc = cuda_check(h, cudaGetLastError(), "k_bl_gram"))) return rc;
   k_bl_mr<L><<<1, 32, 0, h->stream>>>(sc);
   h->launches++;
   if ((rc = cuda_check(h, cudaGetLastError(), "k_bl_mr"))) return rc;
-  k_bl_fin<R, L><<<RED_BLOCKS, VB, 0, h->stream>>>(rs, us, x, n, h->red, sc);
-  h->launches++;
+  launch_wave(h, k_bl_fin<R, L>, RED_BLOCKS, rs, us, x, n, h->red, sc);
   return cuda_check(h, cudaGetLastError(), "k_bl_fin");
 }
 

@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(VB) k_bicg_xr(typename CT<R>::C *x, const type
         r[i] = ri;
         acc(rh[i], ri);
       });
-  block_reduce_finalise<VB, sizeof(R) == 4>(make_double2(a0r.get(), a0i.get()), make_double2(a1.get(), 0.0), red, FIN_XR, sc);
+  sum_finalise<VB>(a0r, a0i, a1, red, FIN_XR, sc);
 }
 
 // Jacobi-preconditioned COCG on the S-symmetric operator (S = V_E, so S·A
@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(VB) k_cocg_xr(typename CT<R>::C *x, const type
     a0i.add(d.y);
     a1.add(ri.x * ri.x + ri.y * ri.y);
   }
-  block_reduce_finalise<VB, sizeof(R) == 4>(make_double2(a0r.get(), a0i.get()), make_double2(a1.get(), 0.0), red, FIN_COCG_R, sc);
+  sum_finalise<VB>(a0r, a0i, a1, red, FIN_COCG_R, sc);
 }
 
 // COCG direction: p = D⁻¹ r + β p
@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(VB) k_dot(const typename CT<R>::C *__restrict_
     a0i.add(d.y);
     a1.add(ai.x * ai.x + ai.y * ai.y);
   }
-  block_reduce_finalise<VB, sizeof(R) == 4>(make_double2(a0r.get(), a0i.get()), make_double2(a1.get(), 0.0), red, FIN_NONE, sc);
+  sum_finalise<VB>(a0r, a0i, a1, red, FIN_NONE, sc);
 }
 
 // pᵀ (S q) (unconjugated, weighted) → FIN_COCG_A
@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(VB) k_dot_u(const typename CT<R>::C *__restric
     a0r.add(d.x);
     a0i.add(d.y);
   }
-  block_reduce_finalise<VB, sizeof(R) == 4>(make_double2(a0r.get(), a0i.get()), make_double2(0.0, 0.0), red, fin, sc);
+  sum_finalise<VB>(a0r, a0i, red, fin, sc);
 }
 
 // ---------------------------------------------------------------- mixed precision

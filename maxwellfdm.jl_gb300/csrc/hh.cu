@@ -194,7 +194,7 @@ __global__ void __launch_bounds__(NTHR, 2) k_apply_hh(OpArgs<R> a, Extra<R> ex, 
     if (k + 1 < k1) load_hplane<R>(S, a, ex, x, i0, j0, k + 2, sm, tid);
   }
   if (EPI != EPI_STORE) {
-    block_reduce_finalise<NTHR, sizeof(R) == 4>(make_double2(r0.get(), i0acc.get()), make_double2(r1.get(), 0.0), red, fin, sc);
+    sum_finalise<NTHR>(r0, i0acc, r1, red, fin, sc);
   }
 }
 

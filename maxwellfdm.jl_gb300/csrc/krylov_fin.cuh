@@ -1,10 +1,12 @@
 // Grid-wide reductions and the scalar recurrences of the Krylov solvers.
 //
-// Every reducing kernel writes two FP64 complex partials per block; the
-// last block to arrive (atomic counter) sums them in block order — so the
-// result is deterministic — and runs the scalar update of the solver step
+// Every reducing kernel writes its partial sums per block; the last block
+// to arrive (atomic counter) sums them in block order — so the result is
+// deterministic — and runs the scalar update of the solver step
 // (finalise).  No block ever waits on another: the counter is only read by
-// the block that incremented it last.
+// the block that incremented it last.  complex128 kernels sum in FP64;
+// complex64 kernels sum in double-float FP32 arithmetic (DF below) up to
+// the single value per sum that is widened for finalise.
 #pragma once
 
 #include "fdfd_internal.cuh"
@@ -133,44 +135,132 @@ __device__ __forceinline__ void two_sum_f(float a, float b, float &s, float &e) 
   e = (a - (s - bb)) + (b - bb);
 }
 
-// Warp sum of a value that carries at most about 48 significant bits (an
-// FP32 sum, or a compensated FP32 sum widened to FP64): split into FP32
-// (hi, lo), add along an FP32 TwoSum tree, widen once.  The GPU's FP64 pipe
-// is a small fraction of its FP32 pipe, so the warp trees of the complex64
-// kernels avoid FP64 additions altogether.
-__device__ __forceinline__ double warp_sum_split(double x) {
-  float hi = (float)x, lo = (float)(x - (double)hi);
+// Double-float value hi + lo: about 48 significant bits carried in FP32
+// arithmetic.  The GPU's FP64 pipe (conversions included) is a small
+// fraction of its FP32 pipe, so the complex64 kernels keep every
+// cross-thread and cross-block sum in this form.
+struct DF {
+  float hi, lo;
+};
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+  float s, e;
+  two_sum_f(a.hi, b.hi, s, e);
+  e += a.lo + b.lo;
+  DF r;
+  two_sum_f(s, e, r.hi, r.lo);
+  return r;
+}
+__device__ __forceinline__ DF df_shfl_xor(DF v, int o) {
+  return DF{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+}
+__device__ __forceinline__ double df_widen(DF v) { return (double)v.hi + (double)v.lo; }
+
+// Warp reduce-scatter of K double-float values per lane (K a power of two,
+// ≤ 32): butterfly levels 16, 8, … each halve the values a lane keeps
+// (lanes with the level's bit set keep the upper half), then plain
+// butterfly levels once one value is left — K−1+(5−log2 K) additions per
+// lane instead of 5K.  Lane l ends with the warp sum of value
+// l >> (5 − log2 K) in v[0]; the order of additions is fixed.
+template <int M, int O>
+struct DfScatter {
+  static __device__ __forceinline__ void run(DF *v, int lane) {
+    if constexpr (M > 1) {
+      const bool up = (lane & O) != 0;
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const float oh = __shfl_xor_sync(0xffffffffu, hi, o), ol = __shfl_xor_sync(0xffffffffu, lo, o);
-    float s, e;
-    two_sum_f(hi, oh, s, e);
-    hi = s;
-    lo = lo + ol + e;
+      for (int i = 0; i < M / 2; ++i) {
+        const DF keep = up ? v[M / 2 + i] : v[i];
+        const DF send = up ? v[i] : v[M / 2 + i];
+        v[i] = df_add(keep, df_shfl_xor(send, O));
+      }
+      DfScatter<M / 2, O / 2>::run(v, lane);
+    } else {
+      v[0] = df_add(v[0], df_shfl_xor(v[0], O));
+      DfScatter<1, O / 2>::run(v, lane);
+    }
   }
-  return (double)hi + (double)lo;
+};
+template <int M>
+struct DfScatter<M, 0> {
+  static __device__ __forceinline__ void run(DF *, int) {}
+};
+template <int K>
+constexpr int df_shift() {
+  return K >= 32 ? 0 : K >= 16 ? 1 : K >= 8 ? 2 : K >= 4 ? 3 : K >= 2 ? 4 : 5;
 }
 
-// Block-level reduction of two complex FP64 values, then the grid-level
-// last-block finalisation.  Must be called by every thread of the block.
-// F32 (complex64 kernels): the warp trees run in FP32 TwoSum arithmetic.
-template <int NT, bool F32 = false>
+// Block and grid sums of KR double-float values per thread (v holds K ≥ KR
+// slots, K a power of two, the slots from KR on zero).  Writes the block's
+// KR partials (float2 each, KR/2 double2 slots of red.part per block) and
+// returns true in the block that arrives last, which then holds the grid
+// sums, widened to FP64, in tot (shared, KR entries).  Every thread of the
+// block must call it.
+template <int NT, int K, int KR>
+__device__ bool df_block_sums_last(DF (&v)[K], RedBuf red, double *tot) {
+  static_assert((K & (K - 1)) == 0 && K <= 32 && KR <= K && (KR % 2) == 0, "DF block sums");
+  constexpr int NW = NT / 32;
+  __shared__ DF wred[NW][K];
+  __shared__ bool last;
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int lane = tid & 31, wid = tid >> 5;
+  DfScatter<K, 16>::run(v, lane);
+  if ((lane & ((1 << df_shift<K>()) - 1)) == 0) wred[wid][lane >> df_shift<K>()] = v[0];
+  __syncthreads();
+  const unsigned nblk = gridDim.x * gridDim.y * gridDim.z;
+  const unsigned bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+  float2 *part = reinterpret_cast<float2 *>(red.part);
+  if (tid < KR) {
+    DF s = wred[0][tid];
+#pragma unroll
+    for (int w = 1; w < NW; ++w) s = df_add(s, wred[w][tid]);
+    part[(long long)KR * bid + tid] = make_float2(s.hi, s.lo);
+    __threadfence();
+  }
+  __syncthreads();
+  if (tid == 0) last = atomicAdd(red.count, 1u) == nblk - 1;
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  // value q is summed by warp q mod NW: lanes over the blocks in a fixed
+  // order, then a fixed butterfly
+  for (int q = wid; q < KR; q += NW) {
+    DF s{0.f, 0.f};
+    for (unsigned b = lane; b < nblk; b += 32) {
+      const float2 p = __ldcg(&part[(long long)KR * b + q]);
+      s = df_add(s, DF{p.x, p.y});
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s = df_add(s, df_shfl_xor(s, o));
+    if (lane == 0) tot[q] = df_widen(s);
+  }
+  __syncthreads();
+  if (tid == 0) *red.count = 0u;
+  return true;
+}
+
+// complex64 kernels: grid sums of the complex a0 and a1 (as four
+// double-float reals), then finalise in the last block.
+template <int NT>
+__device__ inline void block_reduce_finalise_df(DF a0r, DF a0i, DF a1r, DF a1i, RedBuf red, int mode, KScalars *sc) {
+  __shared__ double tot[4];
+  DF v[4] = {a0r, a0i, a1r, a1i};
+  if (!df_block_sums_last<NT, 4, 4>(v, red, tot)) return;
+  if (threadIdx.x + threadIdx.y + threadIdx.z == 0 && sc)
+    finalise(mode, sc, make_double2(tot[0], tot[1]), make_double2(tot[2], tot[3]));
+}
+
+// Block-level reduction of two complex FP64 values (complex128 kernels),
+// then the grid-level last-block finalisation.  Must be called by every
+// thread of the block.
+template <int NT>
 __device__ inline void block_reduce_finalise(double2 a0, double2 a1, RedBuf red, int mode, KScalars *sc) {
   __shared__ double2 wred[NT / 32][2];
   __shared__ bool last;
-  if (F32) {
-    a0.x = warp_sum_split(a0.x);
-    a0.y = warp_sum_split(a0.y);
-    a1.x = warp_sum_split(a1.x);
-    a1.y = warp_sum_split(a1.y);
-  } else {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      a0.x += __shfl_xor_sync(0xffffffffu, a0.x, o);
-      a0.y += __shfl_xor_sync(0xffffffffu, a0.y, o);
-      a1.x += __shfl_xor_sync(0xffffffffu, a1.x, o);
-      a1.y += __shfl_xor_sync(0xffffffffu, a1.y, o);
-    }
+  for (int o = 16; o > 0; o >>= 1) {
+    a0.x += __shfl_xor_sync(0xffffffffu, a0.x, o);
+    a0.y += __shfl_xor_sync(0xffffffffu, a0.y, o);
+    a1.x += __shfl_xor_sync(0xffffffffu, a1.x, o);
+    a1.y += __shfl_xor_sync(0xffffffffu, a1.y, o);
   }
   const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
   const int lane = tid & 31, wid = tid >> 5;
@@ -224,9 +314,9 @@ __device__ inline void block_reduce_finalise(double2 a0, double2 a1, RedBuf red,
 }
 
 // Per-thread accumulator: FP64 for double kernels; for float kernels a
-// compensated (Neumaier) FP32 sum, widened to FP64 before the block
-// reduction — products and the short per-thread sums stay in FP32, every
-// cross-thread and cross-block addition is FP64.
+// compensated (Neumaier) FP32 sum, handed to the block reduction as a
+// double-float — products and per-thread sums in FP32, every cross-thread
+// and cross-block addition in double-float (float kernels) or FP64.
 template <typename R> struct Acc;
 template <> struct Acc<double> {
   double s = 0.0;
@@ -240,12 +330,15 @@ template <> struct Acc<float> {
     c += (fabsf(s) >= fabsf(v)) ? ((s - t) + v) : ((v - t) + s);
     s = t;
   }
-  __device__ __forceinline__ double get() const { return (double)s + (double)c; }
+  __device__ __forceinline__ DF df() const {
+    DF r;
+    two_sum_f(s, c, r.hi, r.lo);
+    return r;
+  }
 };
 
 // Short per-thread sum (the operator kernel's epilogue adds at most
-// 3 × z-chunk terms per thread): plain FP32, widened before the FP64
-// block and grid sums.
+// 3 × z-chunk terms per thread): plain FP32 for float kernels.
 template <typename R> struct ShortAcc;
 template <> struct ShortAcc<double> {
   double s = 0.0;
@@ -255,8 +348,26 @@ template <> struct ShortAcc<double> {
 template <> struct ShortAcc<float> {
   float s = 0.f;
   __device__ __forceinline__ void add(float v) { s += v; }
-  __device__ __forceinline__ double get() const { return (double)s; }
+  __device__ __forceinline__ DF df() const { return DF{s, 0.f}; }
 };
+
+// Grid sums a0 = a0r + i·a0i and a1 (real) of a reducing kernel, then the
+// solver's scalar step `mode` in the last block (the accumulators'
+// precision picks the FP64 or the double-float path).
+template <int NT, typename A, typename B>
+__device__ inline void sum_finalise(const A &a0r, const A &a0i, const B &a1, RedBuf red, int mode, KScalars *sc) {
+  if constexpr (sizeof(a0r.s) == 4)
+    block_reduce_finalise_df<NT>(a0r.df(), a0i.df(), a1.df(), DF{0.f, 0.f}, red, mode, sc);
+  else
+    block_reduce_finalise<NT>(make_double2(a0r.get(), a0i.get()), make_double2(a1.get(), 0.0), red, mode, sc);
+}
+template <int NT, typename A>
+__device__ inline void sum_finalise(const A &a0r, const A &a0i, RedBuf red, int mode, KScalars *sc) {
+  if constexpr (sizeof(a0r.s) == 4)
+    block_reduce_finalise_df<NT>(a0r.df(), a0i.df(), DF{0.f, 0.f}, DF{0.f, 0.f}, red, mode, sc);
+  else
+    block_reduce_finalise<NT>(make_double2(a0r.get(), a0i.get()), make_double2(0.0, 0.0), red, mode, sc);
+}
 
 // Programmatic dependent launch: a kernel lets the next one in the stream
 // start its prologue early (launch_dependents) and waits for the previous

@@ -508,8 +508,7 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2) k_apply(OpArgs<R
     if (k + 1 < k1) load_plane<R, TRANSPOSE>(S.E, a, ex, x, i0, j0, k + 2, sm, tid);
   }
   if (EPI != EPI_STORE) {
-    block_reduce_finalise<NTHR, sizeof(R) == 4>(make_double2(acc.r0.get(), acc.i0.get()), make_double2(acc.r1.get(), 0.0), red, fin,
-                                sc);
+    sum_finalise<NTHR>(acc.r0, acc.i0, acc.r1, red, fin, sc);
   }
 }
 
@@ -730,8 +729,7 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2)
   }
   __syncthreads();  // no thread leaves while warp 0 may still drain copies into this block's memory
   if (EPI != EPI_STORE) {
-    block_reduce_finalise<NTHR, sizeof(R) == 4>(make_double2(acc.r0.get(), acc.i0.get()), make_double2(acc.r1.get(), 0.0), red, fin,
-                                sc);
+    sum_finalise<NTHR>(acc.r0, acc.i0, acc.r1, red, fin, sc);
   }
 }
 
