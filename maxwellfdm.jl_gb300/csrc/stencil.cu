@@ -96,6 +96,17 @@ struct PlainSmem {
   OffTile<R> O;
 };
 
+// Per-chunk copies of the z coefficient arrays and the off-diagonal flags of
+// the tile column, indexed by plane − (k0 − 1) over k0 − 1 … k1 (staged once
+// per CTA, so no plane waits on a global load for them).
+constexpr int KCMAX = 64;  // longest z-chunk (the autotuner's range)
+template <typename R>
+struct ZTile {
+  using C = typename CT<R>::C;
+  C cm[KCMAX + 2], ce[KCMAX + 2], wm[KCMAX + 2], wp[KCMAX + 2];
+  unsigned char flag[KCMAX + 2];
+};
+
 // ---- TMA ring: the global AoS cell layout, 4 slots.  The box starts XOFF
 // cells left of the tile so its x coordinate is 16-byte aligned.
 template <typename R>
@@ -108,6 +119,7 @@ struct TmaGeom {
   static constexpr int H_OFF = NSLOT * SLOT_BYTES;
   static constexpr int T_OFF = H_OFF + (int)((sizeof(HTile<R>) + 15) / 16 * 16);
   static constexpr int O_OFF = T_OFF + (int)((sizeof(CoefTile<R>) + 15) / 16 * 16);
+  static constexpr int Z_OFF = O_OFF + (int)((sizeof(OffTile<R>) + 15) / 16 * 16);
   // complex64 only: a ring slot per plane for the off-diagonal ε of corners
   // i0 … i0+EOX−1, j0 … j0+TY, laid out [p][jj][ii] (EOX·4 bytes a multiple
   // of 16); complex128 reads them from global memory (shared memory would
@@ -116,7 +128,7 @@ struct TmaGeom {
   static constexpr int EO_BYTES = sizeof(R) == 4 ? EOX * (TY + 1) * 3 * (int)sizeof(R) : 0;
   static constexpr int EO_SLOT = (EO_BYTES + 127) / 128 * 128;
   // TMA destinations (E slots, ε slots) start on 128-byte boundaries
-  static constexpr int EO_OFF = (O_OFF + (int)sizeof(OffTile<R>) + 127) / 128 * 128;
+  static constexpr int EO_OFF = (Z_OFF + (int)sizeof(ZTile<R>) + 127) / 128 * 128;
   static constexpr int BAR_OFF = EO_OFF + NSLOT * EO_SLOT;
   static constexpr int SMEM = BAR_OFF + NSLOT * 8 + 128;  // + alignment slack
   static_assert(SLOT_BYTES % 128 == 0 && EO_OFF % 128 == 0 && EO_SLOT % 128 == 0, "TMA destination alignment");
@@ -192,15 +204,14 @@ __device__ __forceinline__ void curl_e(const ET &E, const CoefTile<R> &T, typena
 
 constexpr int H_HALO = TX + TY;  // halo positions: column i = −1 (TY), row j = −1 (TX)
 
-// H(k): every thread at its own cell (kept in `own` and stored for its
+// H(k) (cmz: the z coefficient 1/s∆lₘ of plane k): every thread at its own cell (kept in `own` and stored for its
 // neighbours), threads 0 … TX+TY−1 also at one low-halo position, storing
 // only the components a neighbour reads there (hy, hz on the i = −1
 // column; hx, hz on the j = −1 row).
 template <typename R, bool RC, typename ET>
-__device__ __forceinline__ void compute_h(const ET &E, HTile<R> &H, const CoefTile<R> &T, const OpArgs<R> &a,
-                                          int k, int sk, int sk1, int tx, int ty, int tid, Own<R> &own) {
+__device__ __forceinline__ void compute_h(const ET &E, HTile<R> &H, const CoefTile<R> &T, typename CT<R>::C cmz,
+                                          int sk, int sk1, int tx, int ty, int tid, Own<R> &own) {
   using C = typename CT<R>::C;
-  const C cmz = a.cm[2][cidx(a, 2, k)];
   curl_e<R, RC>(E, T, cmz, sk, sk1, tx, ty, own);
   H.hx[ty + 1][tx + 1] = own.hx;
   H.hy[ty + 1][tx + 1] = own.hy;
@@ -236,7 +247,8 @@ struct EoffSrc {
   }
 };
 
-// x- and y-directed corner terms of plane k (E(k−1), E(k) in slots sm, s0).
+// x- and y-directed corner terms of plane k (E(k−1), E(k) in slots sm, s0;
+// wmz, wpz: the z averaging weights of plane k).
 // A thread owns xc/yc positions t and t + NTHR; all its ε loads are issued
 // before any is used, so their latencies overlap.  The positions beyond
 // NTHR (8 of xc, 32 of yc) go to warps 2 and 3, clear of the two warps that
@@ -245,7 +257,8 @@ constexpr int XC_ROT = 2 * TX;                              // xc extras → war
 constexpr int YC_ROT = 3 * TX;                              // yc extras → warp 3
 template <typename R, typename ET>
 __device__ __forceinline__ void stage_xy(const ET &E, OffTile<R> &O, const CoefTile<R> &T, const OpArgs<R> &a,
-                                         const EoffSrc<R> &src, int i0, int j0, int k, int sm, int s0, int tid) {
+                                         const EoffSrc<R> &src, typename CT<R>::C wmz, typename CT<R>::C wpz, int i0,
+                                         int j0, int k, int sm, int s0, int tid) {
   using C = typename CT<R>::C;
   constexpr int NXC = TY * (TX + 1), NYC = (TY + 1) * TX;
   const int tx0 = (tid + NTHR - XC_ROT) % NTHR, ty0 = (tid + NTHR - YC_ROT) % NTHR;
@@ -271,7 +284,6 @@ __device__ __forceinline__ void stage_xy(const ET &E, OffTile<R> &O, const CoefT
       }
     }
   }
-  const C wmz = a.wm[2][k], wpz = a.wp[2][k];
 #pragma unroll
   for (int r = 0; r < 2; ++r) {
     const int p = tx0 + r * NTHR;
@@ -335,16 +347,16 @@ __device__ __forceinline__ void prefetch(Pre<R> &pf, const OpArgs<R> &a, const t
   }
 }
 
-// y(k) at the thread's cell (gi, gj, k) from shared memory.
+// y(k) at the thread's cell (gi, gj, k) from shared memory (cez: the z
+// coefficient 1/s∆lₑ of plane k).
 template <typename R, int EPI, bool TRANSPOSE, bool RC>
 __device__ __forceinline__ void output_cell(const HTile<R> &H, const CoefTile<R> &T, const OffTile<R> &O,
                                             const OpArgs<R> &a, const Extra<R> &ex, const Pre<R> &pf,
                                             const Own<R> &own, typename CT<R>::C hxkm, typename CT<R>::C hykm,
                                             const typename CT<R>::C *__restrict__ x,
                                             typename CT<R>::C *__restrict__ y, int gi, int gj, int k, int tx, int ty,
-                                            bool offd, Accs<R> &acc) {
+                                            bool offd, typename CT<R>::C cez, Accs<R> &acc) {
   using C = typename CT<R>::C;
-  const C cez = a.ce[2][k];
   const C cex = T.cex[tx + 1], cey = T.cey[ty + 1];
   const C hz00 = own.hz, hzjm = H.hz[ty][tx + 1], hzim = H.hz[ty + 1][tx];
   const C hyk = own.hy, hyim = H.hy[ty + 1][tx];
@@ -486,20 +498,22 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2) k_apply(OpArgs<R
     __syncthreads();  // E(k+1) present; the previous plane's reads of H are done
     Own<R> own;
     const bool rc = rxy && k >= a.rlo[2] && k <= a.rhi[2];
-    if (rc) compute_h<R, true>(S.E, S.H, S.T, a, k, s0, s1, tx, ty, tid, own);
-    else compute_h<R, false>(S.E, S.H, S.T, a, k, s0, s1, tx, ty, tid, own);
+    const typename CT<R>::C cmz = a.cm[2][cidx(a, 2, k)];
+    if (rc) compute_h<R, true>(S.E, S.H, S.T, cmz, s0, s1, tx, ty, tid, own);
+    else compute_h<R, false>(S.E, S.H, S.T, cmz, s0, s1, tx, ty, tid, own);
     const bool offd = offd_on(a, tilecol, k);
     if (offd) {
       const EoffSrc<R> g{nullptr};
-      stage_xy<R>(S.E, S.O, S.T, a, g, i0, j0, k, sm, s0, tid);
+      stage_xy<R>(S.E, S.O, S.T, a, g, a.wm[2][k], a.wp[2][k], i0, j0, k, sm, s0, tid);
       if (!zvalid) stage_z<R>(S.E, S.O, S.T, a, g, i0, j0, k, s0, tid);
       stage_z<R>(S.E, S.O, S.T, a, g, i0, j0, k + 1, s1, tid);
     }
     zvalid = offd;
     __syncthreads();  // H(k), staged corners complete; nobody reads E(k−1) any more
     if (active) {
-      if (rc) output_cell<R, EPI, TRANSPOSE, true>(S.H, S.T, S.O, a, ex, pf, own, hxp, hyp, x, y, gi, gj, k, tx, ty, offd, acc);
-      else output_cell<R, EPI, TRANSPOSE, false>(S.H, S.T, S.O, a, ex, pf, own, hxp, hyp, x, y, gi, gj, k, tx, ty, offd, acc);
+      const typename CT<R>::C cez = a.ce[2][k];
+      if (rc) output_cell<R, EPI, TRANSPOSE, true>(S.H, S.T, S.O, a, ex, pf, own, hxp, hyp, x, y, gi, gj, k, tx, ty, offd, cez, acc);
+      else output_cell<R, EPI, TRANSPOSE, false>(S.H, S.T, S.O, a, ex, pf, own, hxp, hyp, x, y, gi, gj, k, tx, ty, offd, cez, acc);
     }
     hxp = own.hx;
     hyp = own.hy;
@@ -588,13 +602,12 @@ __device__ __forceinline__ void pin_fixup(const TmaE<R> &E, int slot, int i0, in
 // both completing on the slot's mbarrier.
 template <typename R>
 __device__ __forceinline__ void issue_plane(unsigned char *smraw, uint64_t *bars, const CUtensorMap *tmap,
-                                            const CUtensorMap *emap, const OpArgs<R> &a, const Extra<R> &ex,
-                                            long long tilecol, int cx, int cy, int i0, int j0, int k0, int q,
-                                            int slot) {
+                                            const CUtensorMap *emap, const Extra<R> &ex, const ZTile<R> &Z,
+                                            int cx, int cy, int i0, int j0, int k0, int q, int slot) {
   using G = TmaGeom<R>;
   bool eo = false;
-  if (G::EO_SLOT > 0 && ex.eoff_tma && q >= k0)
-    eo = (q < a.N[2] && offd_on(a, tilecol, q)) || (q >= 1 && offd_on(a, tilecol, q - 1));
+  // flags of planes q and q − 1 (table index q − (k0 − 1) and one less)
+  if (G::EO_SLOT > 0 && ex.eoff_tma && q >= k0) eo = Z.flag[q - k0 + 1] || Z.flag[q - k0];
   const uint32_t bar = smem_u32(&bars[slot]);
   mbar_expect(bar, (uint32_t)(G::PLANE_BYTES + (eo ? G::EO_BYTES : 0)));
   tma_copy3d(smem_u32(smraw + slot * G::SLOT_BYTES), tmap, cx, cy, q, bar);
@@ -616,6 +629,7 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2)
   HTile<R> &H = *reinterpret_cast<HTile<R> *>(smraw + G::H_OFF);
   CoefTile<R> &T = *reinterpret_cast<CoefTile<R> *>(smraw + G::T_OFF);
   OffTile<R> &O = *reinterpret_cast<OffTile<R> *>(smraw + G::O_OFF);
+  ZTile<R> &Z = *reinterpret_cast<ZTile<R> *>(smraw + G::Z_OFF);
   uint64_t *bars = reinterpret_cast<uint64_t *>(smraw + G::BAR_OFF);
   pdl_trigger();
 
@@ -641,14 +655,28 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2)
     if (ex.eoff_tma) asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&emap)) : "memory");
   }
   fill_coef<R>(T, a, i0, j0, tid);
+  {
+    // z tables over kfirst … k1 (k1 − kfirst ≤ KCMAX + 1); flags are 0
+    // outside the grid
+    const int t = tid - 128;  // warps 4 … 6, clear of fill_coef's threads
+    const int q = kfirst + t;
+    if (t >= 0 && q <= k1) {
+      Z.cm[t] = a.cm[2][cidx(a, 2, q)];
+      if (q >= 0 && q < a.N[2]) {
+        Z.ce[t] = a.ce[2][q];
+        Z.wm[t] = a.wm[2][q];
+        Z.wp[t] = a.wp[2][q];
+      }
+      Z.flag[t] = (q >= 0 && q < a.N[2] && offd_on(a, tilecol, q)) ? 1 : 0;
+    }
+  }
   pdl_wait();
   if (sc != nullptr && sc->done) return;
   __syncthreads();
   if (tid == 0) {
     for (int p = 0; p < G::NSLOT; ++p) {
       const int q = kfirst + p;
-      if (q <= k1)
-        issue_plane<R>(smraw, bars, &tmap, &emap, a, ex, tilecol, cx, cy, i0, j0, k0, q, p);
+      if (q <= k1) issue_plane<R>(smraw, bars, &tmap, &emap, ex, Z, cx, cy, i0, j0, k0, q, p);
     }
   }
   // Only warp 0 polls the mbarriers; the block then joins at bar.sync, which
@@ -672,7 +700,7 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2)
   typename CT<R>::C hxp, hyp;
   {
     Own<R> o;
-    curl_e<R, false>(E, T, a.cm[2][cidx(a, 2, kfirst)], 0, 1, tx, ty, o);
+    curl_e<R, false>(E, T, Z.cm[0], 0, 1, tx, ty, o);
     hxp = o.hx;
     hyp = o.hy;
   }
@@ -691,18 +719,21 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2)
     __syncthreads();  // E(k+1) present and fixed up; the previous plane's reads of H are done
     Own<R> own;
     const bool rc = rxy && k >= a.rlo[2] && k <= a.rhi[2];
-    if (rc) compute_h<R, true>(E, H, T, a, k, s0, s1, tx, ty, tid, own);
-    else compute_h<R, false>(E, H, T, a, k, s0, s1, tx, ty, tid, own);
-    const bool offd = offd_on(a, tilecol, k);
+    // corner staging first, then H: the values H leaves in registers for the
+    // output stage are then not live across the staging
+    const int zt = k - kfirst;
+    const bool offd = Z.flag[zt] != 0;
     if (offd) {
       const bool eo = G::EO_SLOT > 0 && ex.eoff_tma;
       const EoffSrc<R> e0{eo ? reinterpret_cast<const R *>(smraw + G::EO_OFF + s0 * G::EO_SLOT) : nullptr};
       const EoffSrc<R> e1{eo ? reinterpret_cast<const R *>(smraw + G::EO_OFF + s1 * G::EO_SLOT) : nullptr};
-      stage_xy<R>(E, O, T, a, e0, i0, j0, k, sm, s0, tid);
+      stage_xy<R>(E, O, T, a, e0, Z.wm[zt], Z.wp[zt], i0, j0, k, sm, s0, tid);
       if (!zvalid) stage_z<R>(E, O, T, a, e0, i0, j0, k, s0, tid);
       stage_z<R>(E, O, T, a, e1, i0, j0, k + 1, s1, tid);
     }
     zvalid = offd;
+    if (rc) compute_h<R, true>(E, H, T, Z.cm[zt], s0, s1, tx, ty, tid, own);
+    else compute_h<R, false>(E, H, T, Z.cm[zt], s0, s1, tx, ty, tid, own);
     __syncthreads();  // H(k), staged corners complete; nobody reads E(k−1) any more
     // refill E(k−1)'s slot (and its ε slot) right away: the output stage reads
     // only E(k), H and the staged corners, and the next iteration's first
@@ -711,12 +742,12 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2)
       const int q = k + G::NSLOT - 1;  // the plane this freed slot takes
       if (q <= k1) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        issue_plane<R>(smraw, bars, &tmap, &emap, a, ex, tilecol, cx, cy, i0, j0, k0, q, sm);
+        issue_plane<R>(smraw, bars, &tmap, &emap, ex, Z, cx, cy, i0, j0, k0, q, sm);
       }
     }
     if (active) {
-      if (rc) output_cell<R, EPI, false, true>(H, T, O, a, ex, pf, own, hxp, hyp, x, y, gi, gj, k, tx, ty, offd, acc);
-      else output_cell<R, EPI, false, false>(H, T, O, a, ex, pf, own, hxp, hyp, x, y, gi, gj, k, tx, ty, offd, acc);
+      if (rc) output_cell<R, EPI, false, true>(H, T, O, a, ex, pf, own, hxp, hyp, x, y, gi, gj, k, tx, ty, offd, Z.ce[zt], acc);
+      else output_cell<R, EPI, false, false>(H, T, O, a, ex, pf, own, hxp, hyp, x, y, gi, gj, k, tx, ty, offd, Z.ce[zt], acc);
     }
     hxp = own.hx;
     hyp = own.hy;
@@ -784,7 +815,7 @@ static int kchunk_heuristic(const fdfd_handle *h) {
 }
 
 static int kchunk_for(const fdfd_handle *h, bool c64) {
-  if (h->kc_force > 0) return h->kc_force;
+  if (h->kc_force > 0) return std::min(h->kc_force, KCMAX);
   const int t = h->kc[c64 ? 1 : 0];
   return t > 0 ? t : kchunk_heuristic(h);
 }
