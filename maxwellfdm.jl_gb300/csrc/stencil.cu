@@ -569,26 +569,29 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
 
 // Zero the pinned DOFs of a freshly landed plane (their Cₑ columns are 0):
 // E_y, E_z on x = 0; E_x, E_z on y = 0; E_x, E_y on z = 0 (PEC walls).
+// Run by the warp that waited for the plane (lane, 32 lanes), so the block
+// barrier that follows the wait orders it for every thread.
 template <typename R>
-__device__ __forceinline__ void pin_fixup(const TmaE<R> &E, int slot, int i0, int j0, int q, int tid) {
+__device__ __forceinline__ void pin_fixup(const TmaE<R> &E, int slot, int i0, int j0, int q, int lane) {
   using C = typename CT<R>::C;
   using G = TmaGeom<R>;
+  constexpr int NL = 32;
   const C z = czero<C>();
   if (q == 0) {
-    for (int p = tid; p < G::XW * EY; p += NTHR) {
+    for (int p = lane; p < G::XW * EY; p += NL) {
       const int ii = p % G::XW - G::XOFF, jj = p / G::XW - 1;
       *E.ptr(slot, 0, jj, ii) = z;
       *E.ptr(slot, 1, jj, ii) = z;
     }
   }
   if (i0 == 0) {
-    for (int jj = tid - 1; jj <= TY; jj += NTHR) {
+    for (int jj = lane - 1; jj <= TY; jj += NL) {
       *E.ptr(slot, 1, jj, 0) = z;
       *E.ptr(slot, 2, jj, 0) = z;
     }
   }
   if (j0 == 0) {
-    for (int p = tid; p < G::XW; p += NTHR) {
+    for (int p = lane; p < G::XW; p += NL) {
       const int ii = p - G::XOFF;
       *E.ptr(slot, 0, 0, ii) = z;
       *E.ptr(slot, 2, 0, ii) = z;
@@ -682,19 +685,19 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2)
   // Only warp 0 polls the mbarriers; the block then joins at bar.sync, which
   // orders the landed tile for every thread (polling from all warps would
   // burn issue slots the computing warps need).  Pinned-DOF fix-ups run only
-  // in CTAs that touch the low walls.
+  // in CTAs that touch the low walls, by warp 0 right after its wait (tid is
+  // its lane), before that barrier.
   const bool warp0 = tid < 32;
   const bool wall = (i0 == 0) || (j0 == 0);
   if (warp0) {
     ok = mbar_wait(smem_u32(&bars[0]), 0) && ok;
     ok = mbar_wait(smem_u32(&bars[1]), 0) && ok;
+    if (wall || k0 == 0) {
+      pin_fixup<R>(E, 0, i0, j0, kfirst, tid);
+      pin_fixup<R>(E, 1, i0, j0, k0, tid);
+    }
   }
   __syncthreads();
-  if (wall || k0 == 0) {
-    pin_fixup<R>(E, 0, i0, j0, kfirst, tid);
-    pin_fixup<R>(E, 1, i0, j0, k0, tid);
-    __syncthreads();
-  }
   // H(k0−1) at the thread's own cell (the output of plane k0 reads no
   // neighbour of it)
   typename CT<R>::C hxp, hyp;
@@ -711,10 +714,9 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2)
     const int sm = pm % G::NSLOT, s0 = p0 % G::NSLOT, s1 = p1 % G::NSLOT;
     Pre<R> pf;
     if (active) prefetch<R, EPI>(pf, a, aux0, gi + (long long)a.N[0] * (gj + (long long)a.N[1] * k));
-    if (warp0) ok = mbar_wait(smem_u32(&bars[s1]), (p1 / G::NSLOT) & 1) && ok;
-    if (wall) {
-      __syncthreads();
-      pin_fixup<R>(E, s1, i0, j0, k + 1, tid);
+    if (warp0) {
+      ok = mbar_wait(smem_u32(&bars[s1]), (p1 / G::NSLOT) & 1) && ok;
+      if (wall) pin_fixup<R>(E, s1, i0, j0, k + 1, tid);
     }
     __syncthreads();  // E(k+1) present and fixed up; the previous plane's reads of H are done
     Own<R> own;
