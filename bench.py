@@ -169,6 +169,20 @@ def _cpu_system():
     return _CPU
 
 
+def _cpu_model():
+    """The host CPU's model name (lscpu), else the machine type."""
+    import platform
+    import subprocess
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return platform.processor() or platform.machine()
+
+
 def cpu_sample(seconds=8.0):
     """Time per operator application of the CPU baseline's FP64 BiCGStab(4)
     over a bounded sample (about `seconds` of work, at least 3 cycles)."""
@@ -202,7 +216,8 @@ def run_reference(args):
     t_mv = statistics.median(samples)
     value = t_mv * n_mv
     sample = (f"{args.steps} samples of {r['matvecs']} operator applications of FP64 BiCGStab(4) (complex128 CSR, "
-              f"{r['nnz']} nnz, OpenMP on {r['threads']} host threads, oracle/csr_bicgstab.c) on the same 96^3 "
+              f"{r['nnz']} nnz, OpenMP on {r['threads']} host threads of {os.cpu_count()} ({_cpu_model()}), "
+              f"oracle/csr_bicgstab.c) on the same 96^3 "
               f"system; median {t_mv*1e3:.2f} ms per application projected to {n_mv} applications (the FP64 "
               f"BiCGStab(4) count to 1e-6 for this system)")
     line = {"metric": METRIC, "value": value, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
@@ -324,17 +339,18 @@ def run_ours(args):
             proj = r["t_mv"] * st64["matvecs"]
             cpu = {"value": proj, "unit": "s", "cores": r["threads"], "kind": "port",
                    "sample": (f"{r['matvecs']} operator applications of FP64 BiCGStab(4) on the CPU baseline "
-                              f"(complex128 CSR, {r['nnz']} nnz, OpenMP on {r['threads']} host threads) on the same "
+                              f"(complex128 CSR, {r['nnz']} nnz, OpenMP on {r['threads']} host threads of "
+                              f"{os.cpu_count()}, {_cpu_model()}) on the same "
                               f"system: {r['t_mv']*1e3:.2f} ms per application, projected to the {st64['matvecs']} "
                               f"applications the FP64 GPU solve needed")}
         line = {
             "metric": METRIC, "value": t_mixed, "unit": "s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_mixed * 1e3, "higher_is_better": False, "scaling": "weak",
-            "vs_baseline": None, "dtype": "c64 (FP64 reductions and residual replacement)",
+            "vs_baseline": None, "dtype": "c64 (double-float FP32 reductions, FP64 residual replacement)",
             "data": "synthetic (seeded spheres, seed 1000+rank)",
             "config": {"workload": WORKLOAD, "cells": A.ncell, "unknowns": n, "solver": "BiCGStab(4)",
-                       "tol": tol, "l2": "solve working set > L2 (8 c64 + 3 c128 vectors = 0.5 GB); L2 flushed "
-                                         "by a 256 MiB read before each roofline launch",
+                       "tol": tol, "l2": "solve working set > L2 (12 c64 + 3 c128 vectors = 0.38 GB); L2 "
+                                         "flushed by a 256 MiB read before each roofline launch",
                        "parallelism": "replicas" if ws > 1 else "1 GPU"},
             "fp64_time_s": t_fp64, "mixed_speedup_vs_fp64": t_fp64 / t_mixed,
             "iterations": stats[-1]["iterations"], "fp64_iterations": st64["iterations"],
