@@ -508,20 +508,26 @@ static VSet<typename CT<R>::C> vset(typename CT<R>::C *const *v, int count) {
 }
 
 // Blocks for one full wave of a grid-stride kernel: SM count × its resident
-// blocks per SM (cached per kernel), at most `cap`.
+// blocks per SM (cached per kernel and device), at most `cap`.
 static int wave_blocks(const void *kern, int cap) {
   static std::mutex mu;
-  static std::unordered_map<const void *, int> cache;
+  static std::unordered_map<const void *, int> cache[16];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 16) {
+    cudaGetLastError();
+    return std::min(RED_BLOCKS, cap);
+  }
   std::lock_guard<std::mutex> lock(mu);
-  const auto it = cache.find(kern);
-  if (it != cache.end()) return std::min(it->second, cap);
-  int dev = 0, sms = 0, per = 0;
+  const auto it = cache[dev].find(kern);
+  if (it != cache[dev].end()) return std::min(it->second, cap);
+  int sms = 0, per = 0;
   int b = RED_BLOCKS;
-  if (cudaGetDevice(&dev) == cudaSuccess &&
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, VB, 0) == cudaSuccess && sms * per > 0)
     b = sms * per;
-  cache.emplace(kern, b);
+  else
+    cudaGetLastError();
+  cache[dev].emplace(kern, b);
   return std::min(b, cap);
 }
 
