@@ -103,7 +103,7 @@ typedef struct {
 } fdfd_design;
 
 typedef struct {
-  int32_t method;           /* FDFD_BICGSTAB or FDFD_COCG                              */
+  int32_t method;           /* FDFD_BICGSTABL (default), FDFD_BICGSTAB or FDFD_COCG    */
   int32_t precision;        /* FDFD_PREC_FP64 or FDFD_PREC_MIXED                       */
   double tol;               /* target true relative residual ‖b − A x‖/‖b‖ (FP64)      */
   int64_t maxit;            /* iteration cap                                           */
@@ -235,8 +235,9 @@ int fdfd_corner_mean_dev(fdfd_handle *h, int32_t field, const void *in, void *ou
  * model.jl:238-259) and leaves differentiation to its users.  For A e = b and
  * a real objective L(e), pass g = ∂L/∂e, the Wirtinger derivative
  * ½(∂L/∂Re e − i·∂L/∂Im e) (so that dL = 2·Re(gᵀ de)); e.g. for
- * L = |Fᴴe|², g = conj(Fᴴe)·conj(F).  The call solves Aᵀ λ = g with BiCGSTAB
- * (opts: tol, precision, maxit; opts->transpose is ignored) and returns
+ * L = |Fᴴe|², g = conj(Fᴴe)·conj(F).  The call solves Aᵀ λ = g with
+ * opts->method (BiCGStab(ℓ) or BiCGSTAB; COCG is rejected) and opts' tol,
+ * precision and maxit (opts->transpose is ignored), and returns
  *     grad[c + 3·cell] = dL/dε_cc = 2·Re(ω²·λ_c·e_c)
  * at every E_c sample (∂A/∂ε_cc = −ω²).  e, g: complex (2·3·Ncell doubles);
  * grad: 3·Ncell doubles.  Host buffers. */
