@@ -52,6 +52,26 @@ __device__ __forceinline__ typename CT<R>::C tocr(double2 v) {
   return mk(R(v.x), R(v.y));
 }
 
+// Complex scalars of the recurrence in the kernel's precision (at(i) gives
+// the i-th as double2).  complex64 kernels convert each one once per block
+// into shared memory: an FP64 → FP32 conversion runs on the narrow FP64
+// pipe, and done by every thread it held back the first vector loads by
+// microseconds.  Every thread of the block must call it.
+template <typename R, int NS, typename F>
+__device__ __forceinline__ void scalars(F at, typename CT<R>::C (&out)[NS]) {
+  using C = typename CT<R>::C;
+  if constexpr (sizeof(R) == 8) {
+#pragma unroll
+    for (int i = 0; i < NS; ++i) out[i] = at(i);
+  } else {
+    __shared__ C s[NS];
+    if (threadIdx.x < NS) s[threadIdx.x] = tocr<R>(at(threadIdx.x));
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NS; ++i) out[i] = s[i];
+  }
+}
+
 __device__ __forceinline__ double2 conjd(double2 a) { return make_double2(a.x, -a.y); }
 __device__ __forceinline__ double2 addd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ double2 subd(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
@@ -96,7 +116,9 @@ __global__ void __launch_bounds__(VB) k_bl_u(VSet<typename CT<R>::C> r, VSet<typ
                                              typename CT<R>::C *x, long long n, const KScalars *sc) {
   using C = typename CT<R>::C;
   if (sc->done) return;
-  const C be = tocr<R>(sc->beta), al = tocr<R>(sc->alpha);
+  C ba[2];
+  scalars<R>([&](int i) { return i == 0 ? sc->beta : sc->alpha; }, ba);
+  const C be = ba[0], al = ba[1];
   pairs(
       n,
       [&](long long q) {
@@ -145,7 +167,9 @@ __global__ void __launch_bounds__(VB) k_bl_r(VSet<typename CT<R>::C> r, VSet<typ
                                              const KScalars *sc) {
   using C = typename CT<R>::C;
   if (sc->done) return;
-  const C al = tocr<R>(sc->alpha);
+  C a1[1];
+  scalars<R>([&](int) { return sc->alpha; }, a1);
+  const C al = a1[0];
   pairs(
       n,
       [&](long long q) {
@@ -230,7 +254,9 @@ __global__ void __launch_bounds__(VB, 2) k_bl_gram(VSet<typename CT<R>::C> r, VS
   constexpr int NV = L * (L + 1) / 2 + L;
   constexpr int ND = L > 1 ? L - 1 : 1;  // deferred corrections (L − 1 of them)
   if (sc->done) return;
-  const C al = tocr<R>(sc->alpha);
+  C a1[1];
+  scalars<R>([&](int) { return sc->alpha; }, a1);
+  const C al = a1[0];
   R ar[NV], ai[NV];
 #pragma unroll
   for (int q = 0; q < NV; ++q) ar[q] = ai[q] = R(0);
@@ -404,14 +430,14 @@ __global__ void __launch_bounds__(VB, sizeof(R) == 4 ? 3 : 2) k_bl_fin(VSet<type
                                                   typename CT<R>::C *x, long long n, RedBuf red, KScalars *sc) {
   using C = typename CT<R>::C;
   if (sc->done) return;
-  C cx[L + 1], cr[L + 1], cu[L + 1];
-  const C al = tocr<R>(sc->alpha);
-#pragma unroll
-  for (int k = 0; k <= L; ++k) {
-    cx[k] = tocr<R>(sc->cx[k]);
-    cr[k] = tocr<R>(sc->cr[k]);
-    cu[k] = tocr<R>(sc->cu[k]);
-  }
+  C cs[3 * (L + 1) + 1];
+  scalars<R>(
+      [&](int i) {
+        return i <= L ? sc->cx[i] : i <= 2 * L + 1 ? sc->cr[i - (L + 1)] : i <= 3 * L + 2 ? sc->cu[i - 2 * (L + 1)] : sc->alpha;
+      },
+      cs);
+  const C *cx = cs, *cr = cs + (L + 1), *cu = cs + 2 * (L + 1);
+  const C al = cs[3 * (L + 1)];
   Acc<R> a0r, a0i, a1;
   pairs(
       n,
