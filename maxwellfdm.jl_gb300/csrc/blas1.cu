@@ -31,11 +31,6 @@ int ensure_red(fdfd_handle *h, int blocks) {
 
 template <typename C> __device__ __forceinline__ C ld(const C *p, long long i) { return p[i]; }
 
-template <typename R>
-__device__ __forceinline__ typename CT<R>::C tocr(double2 v) {
-  return mk(R(v.x), R(v.y));
-}
-
 // Two consecutive complex elements (2q, 2q+1) per access: one 16-byte
 // float4 for complex64, two 16-byte double2 for complex128.
 __device__ __forceinline__ void ld2(const float2 *__restrict__ a, long long q, float2 &e0, float2 &e1) {
@@ -73,7 +68,9 @@ __global__ void __launch_bounds__(VB) k_bicg_p(const typename CT<R>::C *__restri
   pdl_trigger();
   pdl_wait();
   if (sc->done) return;
-  const C be = tocr<R>(sc->beta), om = tocr<R>(sc->omega);
+  C bo[2];
+  scalars<R>([&](int i) { return i == 0 ? sc->beta : sc->omega; }, bo);
+  const C be = bo[0], om = bo[1];
   auto one = [&](C ri, C pi, C vi) { return cadd(ri, cmul(be, csub(pi, cmul(om, vi)))); };
   pair_loop(
       n,
@@ -96,7 +93,9 @@ __global__ void __launch_bounds__(VB) k_bicg_s(const typename CT<R>::C *__restri
   pdl_trigger();
   pdl_wait();
   if (sc->done) return;
-  const C al = tocr<R>(sc->alpha);
+  C a1[1];
+  scalars<R>([&](int) { return sc->alpha; }, a1);
+  const C al = a1[0];
   pair_loop(
       n,
       [&](long long q) {
@@ -119,7 +118,9 @@ __global__ void __launch_bounds__(VB) k_bicg_xr(typename CT<R>::C *x, const type
   pdl_trigger();
   pdl_wait();
   if (sc->done) return;
-  const C al = tocr<R>(sc->alpha), om = tocr<R>(sc->omega);
+  C ao[2];
+  scalars<R>([&](int i) { return i == 0 ? sc->alpha : sc->omega; }, ao);
+  const C al = ao[0], om = ao[1];
   Acc<R> a0r, a0i, a1;
   auto acc = [&](C rhi, C ri) {
     const C d = cdotc(rhi, ri);
@@ -163,7 +164,9 @@ __global__ void __launch_bounds__(VB) k_cocg_xr(typename CT<R>::C *x, const type
                                                 KScalars *sc) {
   using C = typename CT<R>::C;
   if (sc->done) return;
-  const C al = tocr<R>(sc->alpha);
+  C as[1];
+  scalars<R>([&](int) { return sc->alpha; }, as);
+  const C al = as[0];
   Acc<R> a0r, a0i, a1;
   for (long long i = blockIdx.x * (long long)VB + threadIdx.x; i < n; i += (long long)gridDim.x * VB) {
     x[i] = cadd(x[i], cmul(al, p[i]));
@@ -185,7 +188,9 @@ __global__ void __launch_bounds__(VB) k_cocg_p(const typename CT<R>::C *__restri
                                                long long n, const KScalars *sc) {
   using C = typename CT<R>::C;
   if (sc->done) return;
-  const C be = tocr<R>(sc->beta);
+  C bs[1];
+  scalars<R>([&](int) { return sc->beta; }, bs);
+  const C be = bs[0];
   for (long long i = blockIdx.x * (long long)VB + threadIdx.x; i < n; i += (long long)gridDim.x * VB)
     p[i] = cadd(cmul(dinv[i], r[i]), cmul(be, p[i]));
 }

@@ -128,6 +128,31 @@ __device__ __forceinline__ typename CT<R>::C shadow(long long dof) {
   return mk(R(re) * R(1.0 / 32768.0), R(im) * R(1.0 / 32768.0));
 }
 
+template <typename R>
+__device__ __forceinline__ typename CT<R>::C tocr(double2 v) {
+  return mk(R(v.x), R(v.y));
+}
+
+// Complex scalars of the recurrence in the kernel's precision (at(i) gives
+// the i-th as double2).  complex64 kernels convert each one once per block
+// into shared memory: an FP64 → FP32 conversion runs on the narrow FP64
+// pipe, and done by every thread it held back the first vector loads by
+// microseconds.  Every thread of the block must call it.
+template <typename R, int NS, typename F>
+__device__ __forceinline__ void scalars(F at, typename CT<R>::C (&out)[NS]) {
+  using C = typename CT<R>::C;
+  if constexpr (sizeof(R) == 8) {
+#pragma unroll
+    for (int i = 0; i < NS; ++i) out[i] = at(i);
+  } else {
+    __shared__ C s[NS];
+    if (threadIdx.x < NS) s[threadIdx.x] = tocr<R>(at(threadIdx.x));
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NS; ++i) out[i] = s[i];
+  }
+}
+
 // Error-free FP32 addition (Knuth's TwoSum): s + e == a + b exactly.
 __device__ __forceinline__ void two_sum_f(float a, float b, float &s, float &e) {
   s = a + b;
