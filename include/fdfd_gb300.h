@@ -222,6 +222,15 @@ void fdfd_default_opts(fdfd_solve_opts *opts);
  * buffers and runs asynchronously on the handle's stream. */
 int fdfd_h_from_e(fdfd_handle *h, const double *e, const double *jm, double *hout);
 int fdfd_h_from_e_dev(fdfd_handle *h, const void *e, const void *jm, void *hout);
+/* E = (−i/ω)·Pε⁻¹·(Cₘ h − jₑ): e_from_h (model.jl:281-284) — the E field of
+ * an H-formulation solution.  Pε must be diagonal (the reference's Pε \ …
+ * divides by it); with off-diagonal ε the call returns FDFD_ERR_UNSUPPORTED.
+ * je may be NULL (jₑ = 0).  hin: complex, 2·3·Ncell doubles (H_w at the H_w
+ * sample); je, eout: the same for E (2D slices: each field's components).
+ * Host buffers; the _dev form takes double2 device buffers (3·Ncell) and
+ * runs asynchronously on the handle's stream. */
+int fdfd_e_from_h(fdfd_handle *h, const double *hin, const double *je, double *eout);
+int fdfd_e_from_h_dev(fdfd_handle *h, const void *hin, const void *je, void *eout);
 /* Corner interpolation of create_Mcs (model.jl:287-306): field = FDFD_EE
  * applies Mcₑ (E_w averaged backward along w onto the primal voxel corner,
  * weights s∆lₘ / (2 s∆lₑ)); FDFD_HH applies Mcₘ (H_w averaged forward along w

@@ -94,6 +94,8 @@ SIGNATURES = {
     "fdfd_h_from_e": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
     "fdfd_set_field_type": (C.c_int, [C.c_void_p, C.c_int32]),
     "fdfd_h_from_e_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fdfd_e_from_h": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
+    "fdfd_e_from_h_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "fdfd_corner_mean": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp]),
     "fdfd_corner_mean_dev": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     "fdfd_design_grad_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -826,6 +826,27 @@ int fdfd_h_from_e(fdfd_handle *h, const double *e, const double *jm, double *hou
   return cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
 }
 
+int fdfd_e_from_h_dev(fdfd_handle *h, const void *hin, const void *je, void *eout) {
+  if (!h || !hin || !eout) return set_error(h, FDFD_ERR_ARG, "null argument");
+  cudaSetDevice(h->dev);
+  return e_from_h_dev_impl(h, (const double2 *)hin, (const double2 *)je, (double2 *)eout);
+}
+
+int fdfd_e_from_h(fdfd_handle *h, const double *hin, const double *je, double *eout) {
+  if (!h || !hin || !eout) return set_error(h, FDFD_ERR_ARG, "null argument");
+  if (h->has_off)
+    return set_error(h, FDFD_ERR_UNSUPPORTED, "e_from_h needs a diagonal ε (Pε \\ …), as in the reference");
+  cudaSetDevice(h->dev);
+  int rc = ensure_scratch(h, false);
+  if (!rc && je) rc = ensure_ve(h);
+  if (rc) return rc;
+  if ((rc = h2d_field(h, hin, h->vx64, field_mask(h, true)))) return rc;
+  if (je && (rc = h2d_field(h, je, h->ve64, field_mask(h, false)))) return rc;
+  if ((rc = e_from_h_dev_impl(h, h->vx64, je ? h->ve64 : nullptr, h->vy64))) return rc;
+  if ((rc = d2h_field(h, h->vy64, eout, field_mask(h, false)))) return rc;
+  return cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
+}
+
 int fdfd_corner_mean_dev(fdfd_handle *h, int32_t field, const void *in, void *out) {
   if (!h || !in || !out) return set_error(h, FDFD_ERR_ARG, "null argument");
   if (field != FDFD_EE && field != FDFD_HH) return set_error(h, FDFD_ERR_ARG, "field must be FDFD_EE or FDFD_HH");

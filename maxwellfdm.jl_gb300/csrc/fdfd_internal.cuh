@@ -184,6 +184,7 @@ int eps_grad_dev_impl(fdfd_handle *h, const double2 *e, const double2 *g, double
 int design_grad_dev_impl(fdfd_handle *h, const double *grad, double *out);
 // fields.cu
 int h_from_e_dev_impl(fdfd_handle *h, const double2 *e, const double2 *jm, double2 *hout);
+int e_from_h_dev_impl(fdfd_handle *h, const double2 *hin, const double2 *je, double2 *eout);
 int corner_mean_dev_impl(fdfd_handle *h, int hfield, const double2 *in, double2 *out);
 // host vectors of a 2D slice carry only some components (fields.cu)
 int field_mask(const fdfd_handle *h, bool hfield);

@@ -1,6 +1,10 @@
 // Field post-processing on the device:
 //   * h_from_e — H = (i/ω)·Pμ⁻¹·(Cₑ e + jₘ)        (src/model/model.jl:276-279,
 //     Pμ = I): the forward-difference curl E→H of the operator, one pass;
+//   * e_from_h — E = (−i/ω)·Pε⁻¹·(Cₘ h − jₑ)       (model.jl:281-284) for a
+//     diagonal Pε: the backward-difference curl H→E of the operator (ghost
+//     H(−1) mirrors H(0) on a symmetry wall, Bloch axes wrap with the phase),
+//     divided by ε at each E sample, one pass;
 //   * corner means — the create_Mcs interpolation (model.jl:287-306):
 //     Mcₑ averages E_w backward along w onto the primal voxel corners with
 //     weights s∆lₘ and 1/s∆lₑ (isfwdₑ = boundft .!= EE = false);
@@ -43,6 +47,40 @@ __global__ void k_h_from_e(OpArgs<double> a, Extra<double> ex, const double2 *__
     for (int c = 0; c < 3; ++c) {
       if (jm) h[c] = cadd(h[c], jm[3 * cell + c]);
       hout[3 * cell + c] = cmul(iow, h[c]);
+    }
+  }
+}
+
+// H_c at the cell one step back along w from `cell` (t: the cell's index
+// along w, stride: the cell stride along w).
+__device__ __forceinline__ double2 h_back(const double2 *__restrict__ hin, const OpArgs<double> &a,
+                                          const Extra<double> &ex, long long cell, int t, int w, long long stride,
+                                          int c) {
+  if (t > 0) return hin[3 * (cell - stride) + c];
+  if (a.bloch[w]) return cmul(hin[3 * (cell + (long long)(a.N[w] - 1) * stride) + c], ex.phinv[w]);
+  return hin[3 * cell + c];  // mirror: H(−1) = H(0)
+}
+
+__global__ void k_e_from_h(OpArgs<double> a, Extra<double> ex, const double2 *__restrict__ hin,
+                           const double2 *__restrict__ je, double2 *__restrict__ eout, double2 miow) {
+  const long long nc = a.ncell;
+  const long long sy = a.N[0], sz = (long long)a.N[0] * a.N[1];
+  for (long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x; cell < nc;
+       cell += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(cell % a.N[0]), j = (int)((cell / a.N[0]) % a.N[1]), k = (int)(cell / sz);
+    const double2 cex = a.ce[0][i], cey = a.ce[1][j], cez = a.ce[2][k];
+    const double2 hx = hin[3 * cell], hy = hin[3 * cell + 1], hz = hin[3 * cell + 2];
+    const double2 hzj = h_back(hin, a, ex, cell, j, 1, sy, 2), hyk = h_back(hin, a, ex, cell, k, 2, sz, 1);
+    const double2 hxk = h_back(hin, a, ex, cell, k, 2, sz, 0), hzi = h_back(hin, a, ex, cell, i, 0, 1, 2);
+    const double2 hyi = h_back(hin, a, ex, cell, i, 0, 1, 1), hxj = h_back(hin, a, ex, cell, j, 1, sy, 0);
+    double2 e[3];
+    e[0] = csub(cmul(cey, csub(hz, hzj)), cmul(cez, csub(hy, hyk)));
+    e[1] = csub(cmul(cez, csub(hx, hxk)), cmul(cex, csub(hz, hzi)));
+    e[2] = csub(cmul(cex, csub(hy, hyi)), cmul(cey, csub(hx, hxj)));
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      if (je) e[c] = csub(e[c], je[3 * cell + c]);
+      eout[3 * cell + c] = cscale(cmul(miow, e[c]), 1.0 / a.eps[c * nc + cell]);
     }
   }
 }
@@ -203,6 +241,20 @@ int h_from_e_dev_impl(fdfd_handle *h, const double2 *e, const double2 *jm, doubl
   k_h_from_e<<<152 * 8, 256, 0, h->stream>>>(a, ex, e, jm, hout, iow);
   h->launches++;
   return cuda_check(h, cudaGetLastError(), "k_h_from_e");
+}
+
+int e_from_h_dev_impl(fdfd_handle *h, const double2 *hin, const double2 *je, double2 *eout) {
+  if (h->has_off)
+    return set_error(h, FDFD_ERR_UNSUPPORTED, "e_from_h needs a diagonal ε (Pε \\ …), as in the reference");
+  const OpArgs<double> a = op_args<double>(h);
+  const Extra<double> ex = make_extra<double>(h);
+  // −i/ω for complex ω
+  const double wr = h->omega[0], wi = h->omega[1], d = wr * wr + wi * wi;
+  if (!(d > 0.0)) return set_error(h, FDFD_ERR_ARG, "e_from_h needs ω ≠ 0");
+  const double2 miow = make_double2(-wi / d, -wr / d);
+  k_e_from_h<<<152 * 8, 256, 0, h->stream>>>(a, ex, hin, je, eout, miow);
+  h->launches++;
+  return cuda_check(h, cudaGetLastError(), "k_e_from_h");
 }
 
 int corner_mean_dev_impl(fdfd_handle *h, int hfield, const double2 *in, double2 *out) {

@@ -9,7 +9,7 @@ module MaxwellFDFDGPU
 using LinearAlgebra
 using MaxwellFDFD
 
-export FDFDOperator, create_A_gpu, SolveOpts, eps_grad, h_from_e, corner_mean
+export FDFDOperator, create_A_gpu, SolveOpts, eps_grad, h_from_e, e_from_h, corner_mean
 
 const libfdfd = joinpath(@__DIR__, "..", "libfdfd_gb300.so")
 
@@ -144,6 +144,14 @@ function h_from_e(A::FDFDOperator, e::Vector{ComplexF64}, jₘ::Union{Nothing,Ve
     check(ccall((:fdfd_h_from_e, libfdfd), Cint, (Ptr{Cvoid}, Ptr{ComplexF64}, Ptr{ComplexF64}, Ptr{ComplexF64}),
                 A.h, e, jₘ === nothing ? C_NULL : jₘ, h), A.h)
     return h
+end
+
+# E = (−i/ω)Pε⁻¹(Cₘh − jₑ) — MaxwellFDFD.e_from_h(h, ω, (Pε,Pμ), (Cₑ,Cₘ), (jₑ,jₘ)) for a diagonal Pε.
+function e_from_h(A::FDFDOperator, h::Vector{ComplexF64}, jₑ::Union{Nothing,Vector{ComplexF64}}=nothing)
+    e = similar(h)
+    check(ccall((:fdfd_e_from_h, libfdfd), Cint, (Ptr{Cvoid}, Ptr{ComplexF64}, Ptr{ComplexF64}, Ptr{ComplexF64}),
+                A.h, h, jₑ === nothing ? C_NULL : jₑ, e), A.h)
+    return e
 end
 
 # Mcₑ*e and Mcₘ*h of MaxwellFDFD.create_Mcs(mdl): fields at the voxel corners.

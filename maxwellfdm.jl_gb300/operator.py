@@ -225,6 +225,19 @@ class FDFDOperator:
         self._check(self._lib.fdfd_h_from_e(self._h, dptr(e), None if jmv is None else dptr(jmv), dptr(out)))
         return out
 
+    def e_from_h(self, h, je=None):
+        """E = (−i/ω)·Pε⁻¹·(Cₘ h − jₑ) (e_from_h, model.jl:281-284; diagonal ε
+        only, as the reference's Pε \\ requires), as a DOF vector."""
+        h = np.ascontiguousarray(h, dtype=np.complex128).reshape(-1)
+        if h.size != self.ncomp_h * self.ncell:
+            raise ValueError("h has the wrong length")
+        jev = None if je is None else np.ascontiguousarray(je, dtype=np.complex128).reshape(-1)
+        if jev is not None and jev.size != self.ncomp_e * self.ncell:
+            raise ValueError("je has the wrong length")
+        out = np.empty(self.ncomp_e * self.ncell, dtype=np.complex128)
+        self._check(self._lib.fdfd_e_from_h(self._h, dptr(h), None if jev is None else dptr(jev), dptr(out)))
+        return out
+
     def corner_mean(self, v, field="E"):
         """create_Mcs corner interpolation (model.jl:287-306): field "E" → Mcₑ v
         (primal corners), "H" → Mcₘ v (dual corners)."""

@@ -496,6 +496,15 @@ def h_from_e(e, omega, Ce, jm_vec=None):
     return (1j / omega) * t
 
 
+def e_from_h(h, omega, eps_diag_vec, Cm, je_vec=None):
+    """E = (−i/ω)·Pε⁻¹·(Cₘ h − jₑ) (model.jl:281-284) with a diagonal Pε
+    given by its values at the E samples (DOF order)."""
+    t = Cm @ h
+    if je_vec is not None:
+        t = t - je_vec
+    return (-1j / omega) * t / np.asarray(eps_diag_vec)
+
+
 def create_Mcs(grid, sdl_e, sdl_m, kbloch=(0.0, 0.0, 0.0)):
     """Corner interpolation (create_Mcs, model.jl:287-306), restated from
     the roles given there — create_mean(isfwd, ∆l, ∆l′⁻¹): the mean of each

@@ -56,3 +56,34 @@ def test_corner_means(pkg, oracle, bloch, kb):
         got = A.corner_mean(v, field)
         assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(ref)), field
     A.close()
+
+
+@pytest.mark.parametrize("bloch,kb", CASES)
+def test_e_from_h(pkg, oracle, bloch, kb):
+    """e_from_h (model.jl:281-284) with a diagonal ε against the oracle, and
+    its rejection of an off-diagonal ε (the reference's Pε \\ needs a
+    diagonal one)."""
+    O = oracle
+    g = _grid(O, bloch)
+    om = 2 * np.pi / 6.5
+    npml = ((0 if bloch[0] else 2, 2, 0 if bloch[2] else 2), (0 if bloch[0] else 2, 2, 0 if bloch[2] else 2))
+    sdl_e, sdl_m = O.stretched_dl(g, om, npml)
+    _, Cm = O.create_curls(g, sdl_e, sdl_m, kb)
+    ph = [np.exp(-1j * kb[w] * g.L[w]) for w in range(3)]
+    A = pkg.FDFDOperator(g.N, om, sdl_e, sdl_m, bloch, ph)
+    rng = np.random.default_rng(34)
+    ed = rng.uniform(1.0, 12.25, g.N + (3,))
+    A.set_eps(ed)
+    n = 3 * g.ncell
+    h = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    je = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    for j in (None, je):
+        ref = O.e_from_h(h, om, O.field_to_vec(ed), Cm, j)
+        got = A.e_from_h(h, j)
+        assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(ref))
+    eo = np.zeros(g.N + (3,))
+    eo[2, 2, 2, 0] = 0.5
+    A.set_eps(ed, eo)
+    with pytest.raises(pkg.FDFDError):
+        A.e_from_h(h)
+    A.close()

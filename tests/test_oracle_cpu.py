@@ -47,6 +47,29 @@ def test_symmetrised_operator(oracle):
     assert np.count_nonzero(S.eps_off) > 0
 
 
+def test_e_from_h_inverts_h_from_e_on_a_solution(oracle):
+    """For A e = b = −iω jₑ with a diagonal Pε (model.jl:264-284):
+    e_from_h(h_from_e(e)) = e exactly, the identity the two restated
+    formulas must satisfy."""
+    import scipy.sparse.linalg as spla
+    O = oracle
+    g = O.uniform_grid((7, 6, 5))
+    om = 2 * np.pi / 4.5
+    S = O.System(g, om, ((1, 2, 1), (2, 1, 1)))
+    rng = np.random.default_rng(41)
+    ed = rng.uniform(1.0, 12.25, g.N + (3,))
+    sdl_e, sdl_m = S.sdl_e, S.sdl_m
+    Ce, Cm = O.create_curls(g, sdl_e, sdl_m)
+    P = O.create_paramop(g, ed, None, sdl_e, sdl_m)
+    A = O.create_A(om, P, Ce, Cm)
+    n = 3 * g.ncell
+    je = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    je[O.field_to_vec(O.pinned_mask(g))] = 0.0
+    e = spla.spsolve(A.tocsc(), O.create_b(om, je))
+    back = O.e_from_h(O.h_from_e(e, om, Ce), om, O.field_to_vec(ed), Cm, je)
+    assert np.max(np.abs(back - e)) <= 1e-9 * np.max(np.abs(e))
+
+
 def test_pinned_rows(oracle):
     """Tangential E on the negative PEC planes: row = −ω² ε, column decoupled."""
     O = oracle
