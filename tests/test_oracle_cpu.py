@@ -70,6 +70,30 @@ def test_e_from_h_inverts_h_from_e_on_a_solution(oracle):
     assert np.max(np.abs(back - e)) <= 1e-9 * np.max(np.abs(e))
 
 
+def test_h_formulation_describes_the_e_solution(oracle):
+    """The oracle's H formulation (create_A_hh, create_b_hh; model.jl:238-240,
+    266-268) solved directly gives h_from_e of the E solution, and e_from_h
+    of it gives the E solution back (diagonal ε, jₘ = 0)."""
+    import scipy.sparse.linalg as spla
+    O = oracle
+    g = O.uniform_grid((6, 7, 5))
+    om = 2 * np.pi / 4.0
+    S = O.System(g, om, ((1, 1, 2), (2, 1, 1)))
+    rng = np.random.default_rng(43)
+    ed = rng.uniform(1.0, 12.25, g.N + (3,))
+    ev = O.field_to_vec(ed)
+    Ce, Cm = O.create_curls(g, S.sdl_e, S.sdl_m)
+    A = O.create_A(om, O.create_paramop(g, ed, None, S.sdl_e, S.sdl_m), Ce, Cm)
+    n = 3 * g.ncell
+    je = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    je[O.field_to_vec(O.pinned_mask(g))] = 0.0
+    e = spla.spsolve(A.tocsc(), O.create_b(om, je))
+    h = spla.spsolve(O.create_A_hh(om, ev, Ce, Cm).tocsc(), O.create_b_hh(om, ev, Ce, je))
+    href = O.h_from_e(e, om, Ce)
+    assert np.max(np.abs(h - href)) <= 1e-9 * np.max(np.abs(href))
+    assert np.max(np.abs(O.e_from_h(h, om, ev, Cm, je) - e)) <= 1e-9 * np.max(np.abs(e))
+
+
 def test_pinned_rows(oracle):
     """Tangential E on the negative PEC planes: row = −ω² ε, column decoupled."""
     O = oracle
