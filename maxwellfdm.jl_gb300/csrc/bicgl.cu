@@ -26,7 +26,8 @@
 // apply them in registers (only r_0, u_0 and x outlive the cycle), which
 // saves nine vector passes per cycle.
 // Vectors and products are in the solve's inner precision; every sum
-// across threads and blocks is FP64, in a fixed order.
+// across threads and blocks is double-float FP32 (complex64) or FP64
+// (complex128), in a fixed order.
 // The grid-stride vector kernels run one full wave (SM count × the
 // kernel's resident blocks per SM), so none ends on a partial wave.
 #include <mutex>

@@ -3,7 +3,7 @@
 //
 // Two precisions share one driver:
 //   FDFD_PREC_FP64   plain complex128 iteration (the comparison baseline);
-//   FDFD_PREC_MIXED  complex64 operator and Krylov vectors, FP64 reductions,
+//   FDFD_PREC_MIXED  complex64 operator and Krylov vectors, ≈48-bit reductions,
 //                    and reliable updates: whenever the recursive residual
 //                    has dropped by δ since the last update, the complex64
 //                    correction is folded into the FP64 solution x64 and the

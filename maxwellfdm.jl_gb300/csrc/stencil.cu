@@ -20,7 +20,8 @@
 //     1/s∆l PML factors, the ε diagonal and — only where the (tile, plane)
 //     flag says so — the corner-averaged off-diagonal ε terms;
 //   * optional fused epilogues produce the dot products a Krylov step needs
-//     (block partials in FP64, last-block finalisation, krylov_fin.cuh);
+//     (block partials in double-float FP32 for complex64, FP64 for
+//     complex128; last-block finalisation, krylov_fin.cuh);
 //   * TRANSPOSE applies Aᵀ = S·A·S⁻¹ with S = V_E (the dual volume of each
 //     E sample), which holds because S·A is complex symmetric.
 #include <cuda.h>
