@@ -180,18 +180,22 @@ int fdfd_matvec_transpose(fdfd_handle *h, const double *x, double *y, int32_t pr
  * that a caller checks a solution against).  Returns once rnorm2 is on the
  * host.  Uses the handle's reduction buffer. */
 int fdfd_residual_dev(fdfd_handle *h, const void *x, const void *b, void *r, double *rnorm2);
-/* Same result as fdfd_residual_dev, for callers that cannot allocate device
- * memory — e.g. a Julia or Python program whose GPU memory is reserved by
- * its framework's caching pool, or a pipelined caller that must not incur
- * the implicit device synchronisation a cudaMalloc/cudaFree can cause.  It
- * has no counterpart in the reference (which never touches a GPU).  The
- * call allocates nothing: its reduction scratch (block partials, arrival
- * counter, result) is a fixed 512 KiB static device array that every GPU
- * loading the library holds until process exit.  Limits: grids needing more
- * than 16384 thread blocks (about 650³ cells) are rejected with
- * FDFD_ERR_ARG.  The first call on a device looks up the array's device
- * address (make it before any stream capture).  All calls share the array:
- * calls that overlap on the GPU race, so serialise them. */
+/* The residual of fdfd_residual_dev (E formulation only; FDFD_ERR_UNSUPPORTED
+ * under FDFD_HH), for callers that cannot allocate device memory — e.g. a
+ * Julia or Python program whose GPU memory is reserved by its framework's
+ * caching pool, or a pipelined caller that must not incur the implicit
+ * device synchronisation a cudaMalloc/cudaFree can cause.  It has no
+ * counterpart in the reference (which never touches a GPU).  The call
+ * allocates nothing: its reduction scratch (block partials, arrival counter,
+ * result) is a fixed 512 KiB static device array that every GPU loading the
+ * library holds until process exit.  It is synchronous: it returns once
+ * rnorm2 is on the host.  Limits: the scratch holds 16384 thread-block
+ * partials; the z-chunk is lengthened as needed, so only grids whose x-y
+ * tiling ⌈Nx/32⌉·⌈Ny/8⌉ exceeds 16384 (more than about 2048×2048 cells per
+ * z-plane) are rejected with FDFD_ERR_ARG.  The first call on a device looks
+ * up the array's device address (make it before any stream capture).  All
+ * calls share the array: calls that overlap on the GPU race, so serialise
+ * them. */
 int fdfd_residual_dev_noalloc(fdfd_handle *h, const void *x, const void *b, void *r, double *rnorm2);
 
 /* ---- solve -----------------------------------------------------------------

@@ -19,9 +19,9 @@ int ensure_red(fdfd_handle *h, int blocks) {
   if (h->red.count) cudaFree(h->red.count);
   h->red.part = nullptr;
   h->red.count = nullptr;
-  cudaError_t e = cudaMalloc(&h->red.part, sizeof(double2) * 2 * (size_t)blocks);
+  cudaError_t e = dev_malloc(&h->red.part, sizeof(double2) * 2 * (size_t)blocks);
   if (e != cudaSuccess) return set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(reduction partials) failed");
-  e = cudaMalloc(&h->red.count, sizeof(unsigned int));
+  e = dev_malloc(&h->red.count, sizeof(unsigned int));
   if (e != cudaSuccess) return set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(reduction counter) failed");
   e = cudaMemsetAsync(h->red.count, 0, sizeof(unsigned int), h->stream);
   if (e != cudaSuccess) return cuda_check(h, e, "cudaMemsetAsync(counter)");

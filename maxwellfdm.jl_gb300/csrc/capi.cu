@@ -28,12 +28,31 @@ int set_error(fdfd_handle *h, int code, const std::string &msg) {
   return code;
 }
 
+cudaError_t dev_malloc_raw(void **p, size_t bytes) {
+  const char *ev = std::getenv("FDFD_FAIL_ALLOC_BYTES");
+  if (ev != nullptr) {
+    const long long lim = std::atoll(ev);
+    if (lim > 0 && bytes >= (size_t)lim) {
+      *p = nullptr;
+      return cudaErrorMemoryAllocation;
+    }
+  }
+  return cudaMalloc(p, bytes);
+}
+
 int cuda_check(fdfd_handle *h, cudaError_t e, const char *what) {
   if (e == cudaSuccess) return FDFD_OK;
   std::string m = std::string(what) + ": " + cudaGetErrorString(e);
   if (e == cudaErrorMemoryAllocation) return set_error(h, FDFD_ERR_NOMEM, m);
   return set_error(h, FDFD_ERR_CUDA, m);
 }
+
+// Make the handle's device current; an entry point returns the failure.
+#define FDFD_SET_DEVICE(h)                                                          \
+  do {                                                                              \
+    const int _rc_dev = cuda_check((h), cudaSetDevice((h)->dev), "cudaSetDevice"); \
+    if (_rc_dev) return _rc_dev;                                                    \
+  } while (0)
 
 int check_dev_err(fdfd_handle *h) {
   if (!h->dev_err) return FDFD_OK;
@@ -142,7 +161,7 @@ int build_oflags(fdfd_handle *h) {
   const int tiles_x = (h->N[0] + TX - 1) / TX, tiles_y = (h->N[1] + TY - 1) / TY;
   const size_t nflag = (size_t)tiles_x * tiles_y * h->N[2];
   if (!h->oflag) {
-    if (cudaMalloc(&h->oflag, nflag) != cudaSuccess) {
+    if (dev_malloc(&h->oflag, nflag) != cudaSuccess) {
       cudaGetLastError();
       return set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(oflag) failed");
     }
@@ -161,15 +180,15 @@ __global__ void k_to_f32(float *dst, const double *src, long long n) {
 static int ensure_eps_buffers(fdfd_handle *h, bool off) {
   const size_t n = 3 * (size_t)h->ncell;
   if (!h->eps64) {
-    if (cudaMalloc(&h->eps64, n * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&h->eps32, n * sizeof(float)) != cudaSuccess) {
+    if (dev_malloc(&h->eps64, n * sizeof(double)) != cudaSuccess ||
+        dev_malloc(&h->eps32, n * sizeof(float)) != cudaSuccess) {
       cudaGetLastError();
       return set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(eps) failed");
     }
   }
   if (off && !h->eoff64) {
-    if (cudaMalloc(&h->eoff64, n * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&h->eoff32, n * sizeof(float)) != cudaSuccess) {
+    if (dev_malloc(&h->eoff64, n * sizeof(double)) != cudaSuccess ||
+        dev_malloc(&h->eoff32, n * sizeof(float)) != cudaSuccess) {
       cudaGetLastError();
       return set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(eps off-diagonal) failed");
     }
@@ -231,15 +250,15 @@ int upload_eps(fdfd_handle *h, const double *eps_diag_aos, const double *eps_off
 static int ensure_scratch(fdfd_handle *h, bool c64) {
   const size_t n = 3 * (size_t)h->ncell;
   if (!h->vx64) {
-    if (cudaMalloc(&h->vx64, n * sizeof(double2)) != cudaSuccess ||
-        cudaMalloc(&h->vy64, n * sizeof(double2)) != cudaSuccess) {
+    if (dev_malloc(&h->vx64, n * sizeof(double2)) != cudaSuccess ||
+        dev_malloc(&h->vy64, n * sizeof(double2)) != cudaSuccess) {
       cudaGetLastError();
       return set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(scratch) failed");
     }
   }
   if (c64 && !h->vx32) {
-    if (cudaMalloc(&h->vx32, n * sizeof(float2)) != cudaSuccess ||
-        cudaMalloc(&h->vy32, n * sizeof(float2)) != cudaSuccess) {
+    if (dev_malloc(&h->vx32, n * sizeof(float2)) != cudaSuccess ||
+        dev_malloc(&h->vy32, n * sizeof(float2)) != cudaSuccess) {
       cudaGetLastError();
       return set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(scratch c64) failed");
     }
@@ -325,6 +344,7 @@ int fdfd_create(const fdfd_desc *d, fdfd_handle **out) {
     return set_error(nullptr, FDFD_ERR_NO_DEVICE, "no CUDA device");
   }
   if (d->device < 0 || d->device >= ndev) return set_error(nullptr, FDFD_ERR_ARG, "bad device ordinal");
+  if (d->device >= MAX_DEVICES) return set_error(nullptr, FDFD_ERR_UNSUPPORTED, "device ordinal above 63");
   fdfd_handle *h = new fdfd_handle();
   h->dev = d->device;
   int rc;
@@ -393,8 +413,8 @@ int fdfd_create(const fdfd_desc *d, fdfd_handle **out) {
     h->rlo[w] = lo < N ? lo : 1;
     h->rhi[w] = lo < N ? hi : 0;
   }
-  if (cudaMalloc(&h->coef64, c64.size() * sizeof(double2)) != cudaSuccess ||
-      cudaMalloc(&h->coef32, c32.size() * sizeof(float2)) != cudaSuccess) {
+  if (dev_malloc(&h->coef64, c64.size() * sizeof(double2)) != cudaSuccess ||
+      dev_malloc(&h->coef32, c32.size() * sizeof(float2)) != cudaSuccess) {
     cudaGetLastError();
     fdfd_destroy(h);
     return set_error(nullptr, FDFD_ERR_NOMEM, "cudaMalloc(coefficients) failed");
@@ -408,13 +428,13 @@ int fdfd_create(const fdfd_desc *d, fdfd_handle **out) {
     cudaMemcpy(h->eps64, ones.data(), ones.size() * sizeof(double), cudaMemcpyHostToDevice);
   }
   if ((rc = finish_eps(h))) { fdfd_destroy(h); return rc; }
-  if (cudaMalloc(&h->util_sc, sizeof(KScalars)) != cudaSuccess) {
+  if (dev_malloc(&h->util_sc, sizeof(KScalars)) != cudaSuccess) {
     cudaGetLastError();
     fdfd_destroy(h);
     return set_error(nullptr, FDFD_ERR_NOMEM, "cudaMalloc(scalars) failed");
   }
   cudaMemsetAsync(h->util_sc, 0, sizeof(KScalars), h->stream);
-  if (cudaMalloc(&h->dev_err, sizeof(int)) != cudaSuccess) {
+  if (dev_malloc(&h->dev_err, sizeof(int)) != cudaSuccess) {
     cudaGetLastError();
     fdfd_destroy(h);
     return set_error(nullptr, FDFD_ERR_NOMEM, "cudaMalloc(error flag) failed");
@@ -429,6 +449,8 @@ int fdfd_create(const fdfd_desc *d, fdfd_handle **out) {
     h->pdl = pd != nullptr && pd[0] != '\0' && pd[0] != '0';
     const char *kc = std::getenv("FDFD_KCHUNK");
     if (kc != nullptr) h->kc_force = std::max(1, std::min(std::atoi(kc), h->N[2]));
+    const char *wl = std::getenv("FDFD_WAIT_LIMIT_CLOCKS");
+    if (wl != nullptr) h->wait_limit = std::max(0ll, std::min(std::atoll(wl), h->wait_limit));
   }
   if ((rc = autotune_kchunk(h))) { fdfd_destroy(h); return rc; }
   if ((rc = ensure_red(h, apply_blocks(h)))) { fdfd_destroy(h); return rc; }
@@ -439,7 +461,7 @@ int fdfd_create(const fdfd_desc *d, fdfd_handle **out) {
 
 void fdfd_destroy(fdfd_handle *h) {
   if (!h) return;
-  cudaSetDevice(h->dev);
+  cudaSetDevice(h->dev);  // best effort: a destructor has no status to return
   if (h->stream) cudaStreamSynchronize(h->stream);
   free_workspace(h);
   if (!h->shares_operator) {
@@ -479,13 +501,13 @@ int fdfd_sync(fdfd_handle *h) {
 
 int fdfd_set_eps(fdfd_handle *h, const double *eps_diag, const double *eps_off) {
   if (!h || !eps_diag) return set_error(h, FDFD_ERR_ARG, "null argument");
-  cudaSetDevice(h->dev);
+  FDFD_SET_DEVICE(h);
   return upload_eps(h, eps_diag, eps_off);
 }
 
 int fdfd_set_eps_tensor(fdfd_handle *h, const double *epsarr) {
   if (!h || !epsarr) return set_error(h, FDFD_ERR_ARG, "null argument");
-  cudaSetDevice(h->dev);
+  FDFD_SET_DEVICE(h);
   const long long nc = h->ncell;
   // column-major (Nx,Ny,Nz,3,3): element (cell, r, c) at cell + nc*(r + 3c)
   auto at = [&](long long cell, int r, int c, int part) { return epsarr[2 * (cell + nc * (r + 3 * c)) + part]; };
@@ -512,13 +534,13 @@ int fdfd_smooth_objects(fdfd_handle *h, const double *const lprim[3], const fdfd
   if (!h || !lprim || (nobj > 0 && !objs) || nobj < 0) return set_error(h, FDFD_ERR_ARG, "bad argument");
   for (int w = 0; w < 3; ++w)
     if (!lprim[w]) return set_error(h, FDFD_ERR_ARG, "null lprim");
-  cudaSetDevice(h->dev);
+  FDFD_SET_DEVICE(h);
   return smooth_objects_impl(h, lprim, objs, nobj, eps_bg, design);
 }
 
 int fdfd_get_eps(fdfd_handle *h, double *eps_diag, double *eps_off, uint8_t *smask) {
   if (!h) return set_error(nullptr, FDFD_ERR_ARG, "null handle");
-  cudaSetDevice(h->dev);
+  FDFD_SET_DEVICE(h);
   const long long nc = h->ncell;
   std::vector<double> soa(3 * (size_t)nc);
   int rc;
@@ -553,19 +575,19 @@ int fdfd_get_eps(fdfd_handle *h, double *eps_diag, double *eps_off, uint8_t *sma
 
 int fdfd_matvec(fdfd_handle *h, const double *x, double *y, int32_t precision) {
   if (!h) return set_error(nullptr, FDFD_ERR_ARG, "null handle");
-  cudaSetDevice(h->dev);
+  FDFD_SET_DEVICE(h);
   return matvec_host(h, x, y, precision, false);
 }
 
 int fdfd_matvec_transpose(fdfd_handle *h, const double *x, double *y, int32_t precision) {
   if (!h) return set_error(nullptr, FDFD_ERR_ARG, "null handle");
-  cudaSetDevice(h->dev);
+  FDFD_SET_DEVICE(h);
   return matvec_host(h, x, y, precision, true);
 }
 
 int fdfd_matvec_dev(fdfd_handle *h, const void *x, void *y, int32_t precision) {
   if (!h || !x || !y) return set_error(h, FDFD_ERR_ARG, "null argument");
-  cudaSetDevice(h->dev);
+  FDFD_SET_DEVICE(h);
   if (precision == FDFD_C64)
     return launch_apply_fin<float>(h, (const float2 *)x, (float2 *)y, EPI_STORE, nullptr, FIN_NONE, nullptr, false);
   if (precision == FDFD_C128)
@@ -576,7 +598,7 @@ int fdfd_matvec_dev(fdfd_handle *h, const void *x, void *y, int32_t precision) {
 
 int fdfd_residual_dev(fdfd_handle *h, const void *x, const void *b, void *r, double *rnorm2) {
   if (!h || !x || !b || !r || !rnorm2) return set_error(h, FDFD_ERR_ARG, "null argument");
-  cudaSetDevice(h->dev);
+  FDFD_SET_DEVICE(h);
   int rc = ensure_red(h, apply_blocks(h));
   if (rc) return rc;
   rc = launch_apply_fin<double>(h, (const double2 *)x, (double2 *)r, EPI_RESID, (const double2 *)b, FIN_NONE,
@@ -619,7 +641,7 @@ int fdfd_solve_dev(fdfd_handle *h, const void *b, void *x, const fdfd_solve_opts
   if (!h || !b || !x) return set_error(h, FDFD_ERR_ARG, "null argument");
   int rc = check_opts(h, opts);
   if (rc) return rc;
-  cudaSetDevice(h->dev);
+  FDFD_SET_DEVICE(h);
   return solve_dev_impl(h, (const double2 *)b, (double2 *)x, opts, stats);
 }
 
@@ -628,7 +650,7 @@ int fdfd_solve(fdfd_handle *h, const double *b, double *x, int32_t nrhs, const f
   if (!h || !b || !x || nrhs < 1) return set_error(h, FDFD_ERR_ARG, "bad argument");
   int rc = check_opts(h, opts);
   if (rc) return rc;
-  cudaSetDevice(h->dev);
+  FDFD_SET_DEVICE(h);
   if ((rc = ensure_scratch(h, false))) return rc;
   const int mask = field_mask(h, h->ft == FDFD_HH);  // the unknown field's components
   const long long n = __builtin_popcount(mask) * h->ncell;  // complex entries per host vector
@@ -690,12 +712,13 @@ static fdfd_handle *make_worker(fdfd_handle *p, int *rc) {
   w->kc[0] = p->kc[0];
   w->kc[1] = p->kc[1];
   w->kc_force = p->kc_force;
+  w->wait_limit = p->wait_limit;
   w->tuned_off = p->tuned_off;
   w->shares_operator = true;
   *rc = FDFD_OK;
   if (cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&w->ev0) != cudaSuccess || cudaEventCreate(&w->ev1) != cudaSuccess ||
-      cudaMalloc(&w->util_sc, sizeof(KScalars)) != cudaSuccess || cudaMalloc(&w->dev_err, sizeof(int)) != cudaSuccess) {
+      dev_malloc(&w->util_sc, sizeof(KScalars)) != cudaSuccess || dev_malloc(&w->dev_err, sizeof(int)) != cudaSuccess) {
     cudaGetLastError();
     *rc = set_error(p, FDFD_ERR_NOMEM, "creating a batch worker failed");
     return w;
@@ -713,7 +736,7 @@ int fdfd_solve_batch(fdfd_handle *h, const double *b, double *x, int32_t nrhs, i
   if (rc) return rc;
   if (nworkers > nrhs) nworkers = nrhs;
   if (nworkers == 1) return fdfd_solve(h, b, x, nrhs, opts, stats);
-  cudaSetDevice(h->dev);
+  FDFD_SET_DEVICE(h);
   if ((rc = cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync"))) return rc;
   std::vector<fdfd_handle *> ws(nworkers, nullptr);
   for (int t = 0; t < nworkers && rc == FDFD_OK; ++t) ws[t] = make_worker(h, &rc);
@@ -726,8 +749,8 @@ int fdfd_solve_batch(fdfd_handle *h, const double *b, double *x, int32_t nrhs, i
     for (int t = 0; t < nworkers; ++t) {
       th.emplace_back([&, t]() {
         fdfd_handle *w = ws[t];
-        cudaSetDevice(w->dev);
-        int r = ensure_scratch(w, false);
+        int r = cuda_check(w, cudaSetDevice(w->dev), "cudaSetDevice");
+        if (r == FDFD_OK) r = ensure_scratch(w, false);
         for (int q = t; q < nrhs && r == FDFD_OK; q += nworkers) {
           if ((r = h2d_field(w, b + 2 * n * q, w->vx64, mask))) break;
           if (opts->x0_given && (r = h2d_field(w, x + 2 * n * q, w->vy64, mask))) break;
@@ -764,7 +787,7 @@ int fdfd_eps_grad_dev(fdfd_handle *h, const void *e, const void *g, void *lam, d
   if (opts->method == FDFD_COCG) return set_error(h, FDFD_ERR_UNSUPPORTED, "the adjoint solve uses BiCGSTAB or BiCGStab(l)");
   if (h->ft != FDFD_EE) return set_error(h, FDFD_ERR_UNSUPPORTED, "the ε gradient is for the E formulation");
   if (!transpose_ok(h)) return set_error(h, FDFD_ERR_UNSUPPORTED, "adjoint with a Bloch phase");
-  cudaSetDevice(h->dev);
+  FDFD_SET_DEVICE(h);
   rc = eps_grad_dev_impl(h, (const double2 *)e, (const double2 *)g, (double2 *)lam, grad, opts, stats);
   if (rc) return rc;
   return cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
@@ -778,10 +801,10 @@ int fdfd_eps_grad(fdfd_handle *h, const double *e, const double *g, double *grad
   if (opts->method == FDFD_COCG) return set_error(h, FDFD_ERR_UNSUPPORTED, "the adjoint solve uses BiCGSTAB or BiCGStab(l)");
   if (h->ft != FDFD_EE) return set_error(h, FDFD_ERR_UNSUPPORTED, "the ε gradient is for the E formulation");
   if (!transpose_ok(h)) return set_error(h, FDFD_ERR_UNSUPPORTED, "adjoint with a Bloch phase");
-  cudaSetDevice(h->dev);
+  FDFD_SET_DEVICE(h);
   if ((rc = ensure_scratch(h, false))) return rc;
   const long long n = 3 * h->ncell;
-  if (!h->ve64 && cudaMalloc(&h->ve64, n * sizeof(double2)) != cudaSuccess) {
+  if (!h->ve64 && dev_malloc(&h->ve64, n * sizeof(double2)) != cudaSuccess) {
     cudaGetLastError();
     h->ve64 = nullptr;
     return set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(adjoint scratch) failed");
@@ -799,7 +822,7 @@ int fdfd_eps_grad(fdfd_handle *h, const double *e, const double *g, double *grad
 
 static int ensure_ve(fdfd_handle *h) {
   if (h->ve64) return FDFD_OK;
-  if (cudaMalloc(&h->ve64, 3 * (size_t)h->ncell * sizeof(double2)) != cudaSuccess) {
+  if (dev_malloc(&h->ve64, 3 * (size_t)h->ncell * sizeof(double2)) != cudaSuccess) {
     cudaGetLastError();
     h->ve64 = nullptr;
     return set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(field scratch) failed");
@@ -809,13 +832,13 @@ static int ensure_ve(fdfd_handle *h) {
 
 int fdfd_h_from_e_dev(fdfd_handle *h, const void *e, const void *jm, void *hout) {
   if (!h || !e || !hout) return set_error(h, FDFD_ERR_ARG, "null argument");
-  cudaSetDevice(h->dev);
+  FDFD_SET_DEVICE(h);
   return h_from_e_dev_impl(h, (const double2 *)e, (const double2 *)jm, (double2 *)hout);
 }
 
 int fdfd_h_from_e(fdfd_handle *h, const double *e, const double *jm, double *hout) {
   if (!h || !e || !hout) return set_error(h, FDFD_ERR_ARG, "null argument");
-  cudaSetDevice(h->dev);
+  FDFD_SET_DEVICE(h);
   int rc = ensure_scratch(h, false);
   if (!rc && jm) rc = ensure_ve(h);
   if (rc) return rc;
@@ -828,7 +851,7 @@ int fdfd_h_from_e(fdfd_handle *h, const double *e, const double *jm, double *hou
 
 int fdfd_e_from_h_dev(fdfd_handle *h, const void *hin, const void *je, void *eout) {
   if (!h || !hin || !eout) return set_error(h, FDFD_ERR_ARG, "null argument");
-  cudaSetDevice(h->dev);
+  FDFD_SET_DEVICE(h);
   return e_from_h_dev_impl(h, (const double2 *)hin, (const double2 *)je, (double2 *)eout);
 }
 
@@ -836,7 +859,7 @@ int fdfd_e_from_h(fdfd_handle *h, const double *hin, const double *je, double *e
   if (!h || !hin || !eout) return set_error(h, FDFD_ERR_ARG, "null argument");
   if (h->has_off)
     return set_error(h, FDFD_ERR_UNSUPPORTED, "e_from_h needs a diagonal ε (Pε \\ …), as in the reference");
-  cudaSetDevice(h->dev);
+  FDFD_SET_DEVICE(h);
   int rc = ensure_scratch(h, false);
   if (!rc && je) rc = ensure_ve(h);
   if (rc) return rc;
@@ -850,14 +873,14 @@ int fdfd_e_from_h(fdfd_handle *h, const double *hin, const double *je, double *e
 int fdfd_corner_mean_dev(fdfd_handle *h, int32_t field, const void *in, void *out) {
   if (!h || !in || !out) return set_error(h, FDFD_ERR_ARG, "null argument");
   if (field != FDFD_EE && field != FDFD_HH) return set_error(h, FDFD_ERR_ARG, "field must be FDFD_EE or FDFD_HH");
-  cudaSetDevice(h->dev);
+  FDFD_SET_DEVICE(h);
   return corner_mean_dev_impl(h, field == FDFD_HH, (const double2 *)in, (double2 *)out);
 }
 
 int fdfd_corner_mean(fdfd_handle *h, int32_t field, const double *in, double *out) {
   if (!h || !in || !out) return set_error(h, FDFD_ERR_ARG, "null argument");
   if (field != FDFD_EE && field != FDFD_HH) return set_error(h, FDFD_ERR_ARG, "field must be FDFD_EE or FDFD_HH");
-  cudaSetDevice(h->dev);
+  FDFD_SET_DEVICE(h);
   int rc = ensure_scratch(h, false);
   if (rc) return rc;
   const int mask = field_mask(h, field == FDFD_HH);
@@ -879,7 +902,7 @@ int fdfd_set_field_type(fdfd_handle *h, int32_t ft) {
 
 int fdfd_design_grad_dev(fdfd_handle *h, const double *grad, double *dgrad) {
   if (!h || !grad || !dgrad) return set_error(h, FDFD_ERR_ARG, "null argument");
-  cudaSetDevice(h->dev);
+  FDFD_SET_DEVICE(h);
   int rc = design_grad_dev_impl(h, grad, dgrad);
   if (rc) return rc;
   return cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
@@ -888,7 +911,7 @@ int fdfd_design_grad_dev(fdfd_handle *h, const double *grad, double *dgrad) {
 int fdfd_design_grad(fdfd_handle *h, const double *grad, double *dgrad) {
   if (!h || !grad || !dgrad) return set_error(h, FDFD_ERR_ARG, "null argument");
   if (!h->has_design) return set_error(h, FDFD_ERR_ARG, "no design region (set one with fdfd_smooth_objects)");
-  cudaSetDevice(h->dev);
+  FDFD_SET_DEVICE(h);
   int rc = ensure_scratch(h, false);
   if (rc) return rc;
   const long long n = 3 * h->ncell;

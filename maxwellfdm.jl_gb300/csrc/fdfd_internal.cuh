@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <string>
 
 #include "../../include/fdfd_gb300.h"
@@ -39,6 +40,18 @@ template <typename C> __host__ __device__ __forceinline__ C cdotc(C a, C b) {
   return mk(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
 }
 template <typename C> __host__ __device__ __forceinline__ C czero() { return mk(decltype(C{}.x)(0), decltype(C{}.x)(0)); }
+
+// Device ordinals a handle may use (fdfd_create rejects larger ones).
+constexpr int MAX_DEVICES = 64;
+
+// One flag per device for a one-time, per-device set-up step (e.g. a
+// kernel's launch attributes).  Atomic: handles on different host threads
+// may reach the step together; the step itself is idempotent.
+struct DevFlags {
+  std::atomic<bool> f[MAX_DEVICES];
+  bool done(int dev) const { return f[dev].load(std::memory_order_acquire); }
+  void set(int dev) { f[dev].store(true, std::memory_order_release); }
+};
 
 // ---------------------------------------------------------------- tiling
 constexpr int TX = 32;   // tile width (x), one warp
@@ -144,6 +157,10 @@ struct fdfd_handle {
   bool pdl = false;                   // programmatic dependent launch (FDFD_PDL=1 enables)
   int kc[2] = {0, 0};                 // tuned z-chunk length: [complex128, complex64]
   int kc_force = 0;                   // FDFD_KCHUNK: fixed z-chunk length (no tuning)
+  // SM clocks a pipeline wait of the TMA operator kernel may take before it
+  // gives up (≈1 s); FDFD_WAIT_LIMIT_CLOCKS lowers it, so that a test can
+  // make a wait run out and see FDFD_ERR_TIMEOUT without hanging anything
+  long long wait_limit = 1ll << 31;
   int tuned_off = -1;                 // has_off at the last tuning (−1: not tuned yet)
   std::string err;
 };
@@ -151,6 +168,14 @@ struct fdfd_handle {
 namespace fdfd {
 
 int set_error(fdfd_handle *h, int code, const std::string &msg);
+// cudaMalloc with a host-side failure hook: while the environment variable
+// FDFD_FAIL_ALLOC_BYTES holds a positive number, every request of at least
+// that many bytes fails with cudaErrorMemoryAllocation without calling the
+// runtime — the way tests exercise FDFD_ERR_NOMEM without exhausting a GPU.
+cudaError_t dev_malloc_raw(void **p, size_t bytes);
+template <typename T> inline cudaError_t dev_malloc(T **p, size_t bytes) {
+  return dev_malloc_raw(reinterpret_cast<void **>(p), bytes);
+}
 int cuda_check(fdfd_handle *h, cudaError_t e, const char *what);
 // FDFD_ERR_TIMEOUT (and clears the flag) if a kernel reported a bounded
 // wait that gave up; call after the stream has been synchronised.

@@ -176,7 +176,7 @@ int field_mask(const fdfd_handle *h, bool hfield) {
 
 static int ensure_stage(fdfd_handle *h) {
   if (h->stage64) return FDFD_OK;
-  if (cudaMalloc(&h->stage64, 3 * (size_t)h->ncell * sizeof(double2)) != cudaSuccess) {
+  if (dev_malloc(&h->stage64, 3 * (size_t)h->ncell * sizeof(double2)) != cudaSuccess) {
     cudaGetLastError();
     h->stage64 = nullptr;
     return set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(2D staging) failed");

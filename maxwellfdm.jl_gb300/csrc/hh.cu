@@ -208,12 +208,11 @@ static int launch_hh_t(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R
     if (rc) return rc;
   }
   const size_t smem = sizeof(HHSmem<R>);
-  static bool attr[8] = {false};
-  const int d = h->dev & 7;
-  if (!attr[d]) {
+  static DevFlags attr;
+  if (!attr.done(h->dev)) {
     cudaError_t e = cudaFuncSetAttribute(k_apply_hh<R, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_check(h, e, "cudaFuncSetAttribute(k_apply_hh)");
-    attr[d] = true;
+    attr.set(h->dev);
   }
   const OpArgs<R> a = op_args<R>(h);
   k_apply_hh<R, EPI><<<grid, dim3(TX, TY, 1), smem, h->stream>>>(a, ex, x, y, aux0, h->red, fin, sc);

@@ -13,8 +13,11 @@
 // library until the process exits.
 //
 // Limits and rules (also stated in include/fdfd_gb300.h):
-//   * at most NOALLOC_MAX_BLOCKS thread blocks (16384: grids up to about
-//     650³ cells); larger grids are rejected with FDFD_ERR_ARG;
+//   * at most NOALLOC_MAX_BLOCKS thread-block partials (16384): the z-chunk
+//     is lengthened until the grid fits, so only an x-y tiling of more than
+//     16384 tiles of 32×8 cells (about 2048×2048 cells per plane) is
+//     rejected with FDFD_ERR_ARG;
+//   * E formulation only; synchronous (returns with ‖r‖² on the host);
 //   * the first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (a host-side name is not a device address); make
 //     that first call before any stream capture;
@@ -40,14 +43,13 @@ constexpr size_t NOALLOC_BYTES = NOALLOC_SC_OFF + ((sizeof(KScalars) + 255) / 25
 // partials [0, 512 KiB) | arrival counter (+256 B) | finalisation scalars
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
 
-constexpr int NOALLOC_MAX_DEVICES = 64;
-static unsigned char *s_scratch[NOALLOC_MAX_DEVICES] = {nullptr};
+static unsigned char *s_scratch[MAX_DEVICES] = {nullptr};
 static std::mutex s_mutex;
 
 // Device address of the scratch array on the current device (looked up once
 // per device, with that device current).
 static int scratch_for(fdfd_handle *h, unsigned char **out) {
-  if (h->dev < 0 || h->dev >= NOALLOC_MAX_DEVICES) return set_error(h, FDFD_ERR_ARG, "device ordinal too large");
+  if (h->dev < 0 || h->dev >= MAX_DEVICES) return set_error(h, FDFD_ERR_ARG, "device ordinal too large");
   std::lock_guard<std::mutex> lock(s_mutex);
   if (!s_scratch[h->dev]) {
     void *p = nullptr;

@@ -15,6 +15,7 @@ struct Extra {
   C ph[3], phinv[3];  // Bloch e^{-ikL} and its inverse
   int kchunk;
   int eoff_tma;       // TMA kernel: off-diagonal ε staged through the shared-memory ring
+  long long wait_limit;  // TMA kernel: SM clocks a pipeline wait may take before it gives up
 };
 
 template <typename R>

@@ -357,7 +357,7 @@ struct DevBuf {
   }
   template <typename T> T *get(fdfd_handle *h, size_t n, int *rc) {
     void *p = nullptr;
-    if (cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) {
+    if (dev_malloc(&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) {
       cudaGetLastError();
       *rc = set_error(h, FDFD_ERR_NOMEM, "cudaMalloc in fdfd_smooth_objects failed");
       return nullptr;
@@ -433,14 +433,14 @@ int smooth_objects_impl(fdfd_handle *h, const double *const lprim[3], const fdfd
   int *oc = buf.get<int>(h, next, &rc);
   unsigned int *dnnz = buf.get<unsigned int>(h, 1, &rc);
   if (!h->smask) {
-    if (cudaMalloc(&h->smask, 4 * (size_t)nc) != cudaSuccess) {
+    if (dev_malloc(&h->smask, 4 * (size_t)nc) != cudaSuccess) {
       cudaGetLastError();
       return set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(smask) failed");
     }
   }
   if (!h->eoff64) {
-    if (cudaMalloc(&h->eoff64, 3 * nc * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&h->eoff32, 3 * nc * sizeof(float)) != cudaSuccess) {
+    if (dev_malloc(&h->eoff64, 3 * nc * sizeof(double)) != cudaSuccess ||
+        dev_malloc(&h->eoff32, 3 * nc * sizeof(float)) != cudaSuccess) {
       cudaGetLastError();
       return set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(eps off-diagonal) failed");
     }

@@ -15,6 +15,7 @@
 // `check_every` iterations is one CUDA graph replay with no host sync;
 // kernels become no-ops once a stop condition is reached inside a batch.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -116,7 +117,7 @@ void drop_graphs(fdfd_handle *h) {
 
 static int alloc(fdfd_handle *h, void **p, size_t bytes, const char *what) {
   if (*p) return FDFD_OK;
-  cudaError_t e = cudaMalloc(p, bytes);
+  cudaError_t e = dev_malloc(p, bytes);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return set_error(h, FDFD_ERR_NOMEM, std::string("cudaMalloc failed for ") + what);
@@ -362,6 +363,10 @@ static int solve_impl(fdfd_handle *h, const double2 *b, double2 *x, const fdfd_s
   TRY(read_scalars(h, ws->scu, &tmp));
   const double bb = tmp.dot1.x;
   st = fdfd_stats{};
+  if (!std::isfinite(bb)) {
+    st.status = FDFD_ERR_NONFINITE;
+    return set_error(h, FDFD_ERR_NONFINITE, "the right-hand side holds a NaN or Inf");
+  }
   if (!(bb > 0.0)) {
     TRY(cuda_check(h, cudaMemsetAsync(x, 0, n * sizeof(double2), h->stream), "zero x"));
     st.status = FDFD_OK;
@@ -371,6 +376,10 @@ static int solve_impl(fdfd_handle *h, const double2 *b, double2 *x, const fdfd_s
   double rr;
   TRY(true_residual(h, b, tr, &rr));
   st.matvecs = 1;
+  if (!std::isfinite(rr)) {
+    st.status = FDFD_ERR_NONFINITE;
+    return set_error(h, FDFD_ERR_NONFINITE, "the initial residual holds a NaN or Inf (check x0)");
+  }
   KScalars &hs = ws->host[0];
   std::memset(&hs, 0, sizeof(KScalars));
   hs.bb = bb;

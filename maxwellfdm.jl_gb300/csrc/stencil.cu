@@ -552,9 +552,20 @@ __device__ __forceinline__ void tma_copy4d(uint32_t dst, const CUtensorMap *map,
       "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
       : "memory");
 }
-// Bounded wait on an mbarrier phase: gives up after ~2^31 SM clocks (about
-// one second) and reports false instead of spinning forever.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+// Bounded wait on an mbarrier phase: gives up after `limit` SM clocks
+// (WAIT_LIMIT ≈ 2^31, about one second) and reports false instead of
+// spinning forever.  limit = 0 tests the phase once without waiting.
+constexpr long long WAIT_LIMIT = 1ll << 31;
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long long limit = WAIT_LIMIT) {
+  if (limit <= 0) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return done != 0;
+  }
   const long long t0 = clock64();
   while (true) {
     uint32_t done;
@@ -564,7 +575,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
         : "r"(bar), "r"(parity)
         : "memory");
     if (done) return true;
-    if (clock64() - t0 > (1ll << 31)) return false;
+    if (clock64() - t0 > limit) return false;
   }
 }
 
@@ -688,17 +699,23 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2)
   // burn issue slots the computing warps need).  Pinned-DOF fix-ups run only
   // in CTAs that touch the low walls, by warp 0 right after its wait (tid is
   // its lane), before that barrier.
+  // A wait that gives up stops the whole block at the next barrier
+  // (__syncthreads_and), so no further copy is issued into a slot whose
+  // previous copy may still be in flight; the block then drains what it
+  // issued (below) and reports FDFD_ERR_TIMEOUT through errflag.
   const bool warp0 = tid < 32;
   const bool wall = (i0 == 0) || (j0 == 0);
   if (warp0) {
-    ok = mbar_wait(smem_u32(&bars[0]), 0) && ok;
-    ok = mbar_wait(smem_u32(&bars[1]), 0) && ok;
-    if (wall || k0 == 0) {
+    ok = mbar_wait(smem_u32(&bars[0]), 0, ex.wait_limit);
+    ok = ok && mbar_wait(smem_u32(&bars[1]), 0, ex.wait_limit);
+    // planes kfirst = k0 − 1 and k0: the z = 0 wall plane is among them when k0 ≤ 1
+    if (ok && (wall || k0 <= 1)) {
       pin_fixup<R>(E, 0, i0, j0, kfirst, tid);
       pin_fixup<R>(E, 1, i0, j0, k0, tid);
     }
   }
-  __syncthreads();
+  int kstop = k0;  // planes up to kstop + 2 have been issued
+  bool run = __syncthreads_and(ok) != 0;
   // H(k0−1) at the thread's own cell (the output of plane k0 reads no
   // neighbour of it)
   typename CT<R>::C hxp, hyp;
@@ -710,16 +727,21 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2)
   }
   bool zvalid = false;  // zc[k & 1] already holds plane k's z-directed corners
 
-  for (int k = k0; k < k1; ++k) {
+  for (int k = k0; run && k < k1; ++k) {
     const int pm = k - 1 - kfirst, p0 = k - kfirst, p1 = k + 1 - kfirst;
     const int sm = pm % G::NSLOT, s0 = p0 % G::NSLOT, s1 = p1 % G::NSLOT;
     Pre<R> pf;
     if (active) prefetch<R, EPI>(pf, a, aux0, gi + (long long)a.N[0] * (gj + (long long)a.N[1] * k));
     if (warp0) {
-      ok = mbar_wait(smem_u32(&bars[s1]), (p1 / G::NSLOT) & 1) && ok;
-      if (wall) pin_fixup<R>(E, s1, i0, j0, k + 1, tid);
+      ok = mbar_wait(smem_u32(&bars[s1]), (p1 / G::NSLOT) & 1, ex.wait_limit);
+      if (ok && wall) pin_fixup<R>(E, s1, i0, j0, k + 1, tid);
     }
-    __syncthreads();  // E(k+1) present and fixed up; the previous plane's reads of H are done
+    // E(k+1) present and fixed up; the previous plane's reads of H are done
+    if (!__syncthreads_and(ok)) {
+      run = false;
+      kstop = k;
+      break;
+    }
     Own<R> own;
     const bool rc = rxy && k >= a.rlo[2] && k <= a.rhi[2];
     // corner staging first, then H: the values H leaves in registers for the
@@ -755,13 +777,19 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2)
     hxp = own.hx;
     hyp = own.hy;
   }
-  if (!ok) {
-    // a bounded wait gave up (warp 0 only): report it and drain this
-    // block's copies, again with bounded waits
-    if (tid == 0) atomicExch(errflag, 1);
-    for (int s = 0; s < G::NSLOT; ++s) mbar_wait(smem_u32(&bars[s]), 0), mbar_wait(smem_u32(&bars[s]), 1);
+  if (!run) {
+    // a bounded wait gave up: report it and wait (with the full limit) for
+    // the last copy issued into each slot — planes kfirst … min(k1, kstop+2),
+    // plane q in slot (q − kfirst) mod NSLOT as phase (q − kfirst) / NSLOT —
+    // so no copy lands in this block's shared memory after it exits
+    if (tid == 0) {
+      atomicExch(errflag, 1);
+      const int qlast = min(k1, kstop + 2);
+      for (int q = max(kfirst, qlast - G::NSLOT + 1); q <= qlast; ++q)
+        mbar_wait(smem_u32(&bars[(q - kfirst) % G::NSLOT]), ((q - kfirst) / G::NSLOT) & 1);
+    }
   }
-  __syncthreads();  // no thread leaves while warp 0 may still drain copies into this block's memory
+  __syncthreads();  // no thread leaves while tid 0 may still drain copies into this block's memory
   if (EPI != EPI_STORE) {
     sum_finalise<NTHR>(acc.r0, acc.i0, acc.r1, red, fin, sc);
   }
@@ -838,6 +866,7 @@ Extra<R> make_extra(const fdfd_handle *h) {
   Extra<R> ex;
   ex.kchunk = kchunk_for(h, sizeof(R) == 4);
   ex.eoff_tma = 0;
+  ex.wait_limit = h->wait_limit;
   const C *coef;
   if constexpr (sizeof(R) == 8) coef = reinterpret_cast<const C *>(h->coef64);
   else coef = reinterpret_cast<const C *>(h->coef32);
@@ -855,18 +884,16 @@ template Extra<float> make_extra<float>(const fdfd_handle *);
 template Extra<double> make_extra<double>(const fdfd_handle *);
 
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  static bool tried = false;
-  if (!tried) {
-    tried = true;
+  // resolved once (a function-local static is initialised thread-safely)
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
     void *p = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
-    else
-      cudaGetLastError();
-  }
+      return (PFN_cuTensorMapEncodeTiled_v12000)p;
+    cudaGetLastError();
+    return nullptr;
+  }();
   return fn;
 }
 
@@ -927,18 +954,18 @@ static int launch_t(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R>::
     int rc = ensure_red(h, (int)(grid.x * grid.y * grid.z));
     if (rc) return rc;
   }
-  const int d = h->dev & 7;
+  const int d = h->dev;
   if (!TR && tma_ok<R>(h, x, TR)) {
-    static bool attr_tma[8] = {false};
+    static DevFlags attr_tma;
     const int smem = TmaGeom<R>::SMEM;
-    if (!attr_tma[d]) {
+    if (!attr_tma.done(d)) {
       cudaError_t e = cudaFuncSetAttribute(k_apply_tma<R, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
       if (e != cudaSuccess) return cuda_check(h, e, "cudaFuncSetAttribute(k_apply_tma)");
       // shared memory, not L1, limits how many CTAs fit on an SM
       e = cudaFuncSetAttribute(k_apply_tma<R, EPI>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                cudaSharedmemCarveoutMaxShared);
       if (e != cudaSuccess) return cuda_check(h, e, "cudaFuncSetAttribute(carveout)");
-      attr_tma[d] = true;
+      attr_tma.set(d);
     }
     CUtensorMap map, emap;
     int rc = make_map<R>(h, x, &map);
@@ -953,12 +980,12 @@ static int launch_t(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R>::
     h->launches++;
     return cuda_check(h, e, "k_apply_tma launch");
   }
-  static bool attr_set[8] = {false};  // per device ordinal (≤ 8 devices per process)
+  static DevFlags attr_set;
   const size_t smem = sizeof(PlainSmem<R>);
-  if (!attr_set[d]) {
+  if (!attr_set.done(d)) {
     cudaError_t e = cudaFuncSetAttribute(k_apply<R, EPI, TR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_check(h, e, "cudaFuncSetAttribute(k_apply)");
-    attr_set[d] = true;
+    attr_set.set(d);
   }
   const cudaError_t e = launch_k(h, k_apply<R, EPI, TR>, grid, block, smem, a, ex, x, y, aux0, h->red, fin, sc);
   h->launches++;
@@ -977,8 +1004,8 @@ int autotune_kchunk(fdfd_handle *h) {
   const size_t n = 3 * (size_t)h->ncell;
   const size_t flush_bytes = 192ull << 20;
   void *bx = nullptr, *by = nullptr, *fl = nullptr;
-  if (cudaMalloc(&bx, n * sizeof(double2)) != cudaSuccess || cudaMalloc(&by, n * sizeof(double2)) != cudaSuccess ||
-      cudaMalloc(&fl, flush_bytes) != cudaSuccess) {
+  if (dev_malloc(&bx, n * sizeof(double2)) != cudaSuccess || dev_malloc(&by, n * sizeof(double2)) != cudaSuccess ||
+      dev_malloc(&fl, flush_bytes) != cudaSuccess) {
     cudaGetLastError();
     cudaFree(bx);
     cudaFree(by);
@@ -1036,15 +1063,25 @@ int autotune_kchunk(fdfd_handle *h) {
 
 // FP64 residual launcher whose block partials, arrival counter and
 // finalisation scalars live in caller-provided device memory (used by the
-// allocation-free entry point).  Fails if the grid needs more than
-// `max_blocks` partial slots.
+// allocation-free entry point).  The plain-load kernel takes any z-chunk
+// length, so when the tuned chunk would need more than `max_blocks` partial
+// slots the chunk is lengthened (up to the whole z extent) until the grid
+// fits; only an (x, y) tiling larger than `max_blocks` is rejected.
 int launch_residual_ext(fdfd_handle *h, const double2 *x, double2 *r, const double2 *b, RedBuf red, int max_blocks,
                         KScalars *sc) {
   const size_t smem = sizeof(PlainSmem<double>);
   cudaError_t e =
       cudaFuncSetAttribute(k_apply<double, EPI_RESID, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_check(h, e, "cudaFuncSetAttribute(k_apply)");
-  const Extra<double> ex = make_extra<double>(h);
+  Extra<double> ex = make_extra<double>(h);
+  const long long tiles = (long long)((h->N[0] + TX - 1) / TX) * ((h->N[1] + TY - 1) / TY);
+  if (tiles > max_blocks)
+    return set_error(h, FDFD_ERR_ARG, "the grid's x-y tiling needs more thread blocks than the fixed reduction "
+                                      "scratch holds");
+  // smallest chunk length at or above the tuned one whose grid fits
+  const long long zmax = max_blocks / tiles;  // ≥ 1
+  const int kmin = (int)((h->N[2] + zmax - 1) / zmax);
+  if (ex.kchunk < kmin) ex.kchunk = kmin;
   dim3 grid((h->N[0] + TX - 1) / TX, (h->N[1] + TY - 1) / TY, (h->N[2] + ex.kchunk - 1) / ex.kchunk);
   if ((long long)grid.x * grid.y * grid.z > max_blocks)
     return set_error(h, FDFD_ERR_ARG, "grid needs more thread blocks than the fixed reduction scratch holds");

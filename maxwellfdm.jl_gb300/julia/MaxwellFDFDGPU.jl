@@ -2,14 +2,18 @@
 #
 # A GPU operator type that is a drop-in for the SparseMatrixCSC that
 # MaxwellFDFD.create_A returns (src/model/model.jl:238-259): it implements
-# size, eltype, mul!, *, transpose-mul, ldiv!/\ (GPU Krylov solve) and an
-# rrule for the solve.  Signatures mirror include/fdfd_gb300.h one for one.
+# size, eltype, mul!, *, transpose-mul, ldiv!/\ (GPU Krylov solve) and a
+# ChainRulesCore.rrule for the solve with respect to ε and b.  Signatures
+# mirror include/fdfd_gb300.h one for one.
 module MaxwellFDFDGPU
 
 using LinearAlgebra
 using MaxwellFDFD
+import ChainRulesCore
+using ChainRulesCore: NoTangent, unthunk
 
-export FDFDOperator, create_A_gpu, SolveOpts, eps_grad, h_from_e, e_from_h, corner_mean
+export FDFDOperator, create_A_gpu, SolveOpts, eps_grad, h_from_e, e_from_h, corner_mean, solve_with_eps,
+       residual_dev!, residual_dev_noalloc!
 
 const libfdfd = joinpath(@__DIR__, "..", "libfdfd_gb300.so")
 
@@ -64,6 +68,7 @@ mutable struct FDFDOperator <: AbstractMatrix{ComplexF64}
     h::Ptr{Cvoid}
     n::Int
     N::NTuple{3,Int}
+    ω::ComplexF64
 end
 
 Base.size(A::FDFDOperator) = (A.n, A.n)
@@ -84,7 +89,7 @@ function create_A_gpu(mdl::MaxwellFDFD.ModelFull, ω::Number; device::Integer=0)
     GC.@preserve se sm begin
         check(ccall((:fdfd_create, libfdfd), Cint, (Ref{FDFDDesc}, Ref{Ptr{Cvoid}}), d, h), C_NULL)
     end
-    A = FDFDOperator(h[], 3prod(N), N)
+    A = FDFDOperator(h[], 3prod(N), N, ComplexF64(ω))
     finalizer(A -> ccall((:fdfd_destroy, libfdfd), Cvoid, (Ptr{Cvoid},), A.h), A)
     MaxwellFDFD.calc_matparams!(mdl)
     check(ccall((:fdfd_set_eps_tensor, libfdfd), Cint, (Ptr{Cvoid}, Ptr{ComplexF64}), A.h, mdl.εarr), A.h)
@@ -116,15 +121,77 @@ LinearAlgebra.ldiv!(x::Vector{ComplexF64}, A::FDFDOperator, b::Vector{ComplexF64
 Base.:\(A::FDFDOperator, b::Vector{ComplexF64}) = ldiv!(zeros(ComplexF64, length(b)), A, b)
 
 # Adjoint of e = A \ b for a real objective L(e): with g = ∂L/∂e (Wirtinger
-# derivative, dL = 2Re(gᵀde)), λ solves transpose(A) λ = g and ∂L/∂b = λ;
-# ∂L/∂A enters through ε (eps_grad below).  Written against ChainRulesCore
-# when it is loaded.
+# derivative, dL = 2Re(gᵀde)), λ solves transpose(A) λ = g on the GPU.
 function solve_pullback(A::FDFDOperator, e::Vector{ComplexF64}, g::Vector{ComplexF64}; opts::SolveOpts=SolveOpts())
     λ = zeros(ComplexF64, length(g))
     o = SolveOpts(opts.method, opts.precision, opts.tol, opts.maxit, opts.delta, 0, opts.check_every, 1,
                   opts.use_graph, opts.ell)
     solve!(λ, A, g; opts=o)
     return λ
+end
+
+# Replace the diagonal of ε: ε_cc at every E_c sample (3·Ncell reals in the DOF
+# order c + 3·cell); the off-diagonal terms stay as they are.
+function set_eps_diag!(A::FDFDOperator, ε::Vector{Float64})
+    length(ε) == A.n || throw(DimensionMismatch("ε needs one value per E sample"))
+    off = zeros(Float64, A.n)   # ε_xy, ε_yz, ε_zx at each cell's corner, read back and passed on unchanged
+    check(ccall((:fdfd_get_eps, libfdfd), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{UInt8}),
+                A.h, C_NULL, off, C_NULL), A.h)
+    check(ccall((:fdfd_set_eps, libfdfd), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}), A.h, ε, off), A.h)
+    return A
+end
+
+# e = A(ε) \ b with the diagonal ε given per E sample: the differentiable form
+# of the solve (ε enters A = Cₘ Cₑ − ω² Pε, src/model/model.jl:235-237).
+function solve_with_eps(A::FDFDOperator, ε::Vector{Float64}, b::Vector{ComplexF64}; opts::SolveOpts=SolveOpts())
+    set_eps_diag!(A, ε)
+    return first(solve!(zeros(ComplexF64, length(b)), A, b; opts=opts))
+end
+
+# Reverse rule of solve_with_eps, in ChainRulesCore's convention for complex
+# values (a cotangent ē satisfies dL = Re(ēᴴ de)).  With g = conj(ē)/2 the
+# Wirtinger derivative and transpose(A) λ = g solved on the GPU:
+#   ∂A/∂ε_cc = −ω² on the diagonal  ⇒  ε̄_cc = 2Re(ω² λ_c e_c),
+#   e = A⁻¹ b                      ⇒  b̄ = 2 conj(λ).
+function ChainRulesCore.rrule(::typeof(solve_with_eps), A::FDFDOperator, ε::Vector{Float64},
+                              b::Vector{ComplexF64}; opts::SolveOpts=SolveOpts())
+    e = solve_with_eps(A, ε, b; opts=opts)
+    function solve_with_eps_pullback(ē)
+        g = conj.(unthunk(ē)) ./ 2
+        λ = solve_pullback(A, e, g; opts=opts)
+        ε̄ = 2 .* real.((A.ω^2) .* λ .* e)
+        b̄ = 2 .* conj.(λ)
+        return NoTangent(), NoTangent(), ε̄, b̄
+    end
+    return e, solve_with_eps_pullback
+end
+
+# Reverse rule of A \ b with respect to b (A held fixed): b̄ = 2 conj(λ).
+function ChainRulesCore.rrule(::typeof(\), A::FDFDOperator, b::Vector{ComplexF64})
+    e = A \ b
+    function ldiv_pullback(ē)
+        λ = solve_pullback(A, e, conj.(unthunk(ē)) ./ 2)
+        return NoTangent(), NoTangent(), 2 .* conj.(λ)
+    end
+    return e, ldiv_pullback
+end
+
+# True residual r = b − A x and ‖r‖² on device buffers (CUDA.jl CuArray
+# pointers, interleaved complex128): fdfd_residual_dev grows the handle's
+# reduction buffer on first use; fdfd_residual_dev_noalloc allocates nothing
+# (its scratch is a fixed static device array; E formulation only, grids up
+# to 16384 x-y tiles of 32×8 cells).  Both return after ‖r‖² is on the host.
+function residual_dev!(A::FDFDOperator, r::Ptr{Cvoid}, x::Ptr{Cvoid}, b::Ptr{Cvoid})
+    nrm2 = Ref{Float64}(0.0)
+    check(ccall((:fdfd_residual_dev, libfdfd), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ref{Float64}),
+                A.h, x, b, r, nrm2), A.h)
+    return nrm2[]
+end
+function residual_dev_noalloc!(A::FDFDOperator, r::Ptr{Cvoid}, x::Ptr{Cvoid}, b::Ptr{Cvoid})
+    nrm2 = Ref{Float64}(0.0)
+    check(ccall((:fdfd_residual_dev_noalloc, libfdfd), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ref{Float64}), A.h, x, b, r, nrm2), A.h)
+    return nrm2[]
 end
 
 # dL/dε_cc = 2Re(ω²λ_c e_c) at every E_c sample, as a (3, Nx, Ny, Nz) array

@@ -208,8 +208,11 @@ class FDFDOperator:
                        kw.get("check_every", 50), kw.get("transpose", False), kw.get("use_graph", True),
                        kw.get("ell", 4))
         st = _lib.fdfd_stats()
-        self._check(self._lib.fdfd_solve_dev(self._h, C.c_void_p(b_ptr), C.c_void_p(x_ptr), C.byref(o),
-                                             C.byref(st)))
+        rc = self._lib.fdfd_solve_dev(self._h, C.c_void_p(b_ptr), C.c_void_p(x_ptr), C.byref(o), C.byref(st))
+        if rc != _lib.FDFD_OK:
+            err = _lib.FDFDError(rc, (self._lib.fdfd_last_error(self._h) or b"").decode())
+            err.stats = st.as_dict()   # iterations, applications and the final true residual so far
+            raise err
         return st.as_dict()
 
     # ---------------------------------------------------------------- fields

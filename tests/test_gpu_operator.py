@@ -185,3 +185,22 @@ def test_tma_and_plain_kernels_agree(pkg, oracle, kind, monkeypatch):
     assert np.array_equal(A1.matvec(x, "c64"), A2.matvec(x, "c64"))
     A1.close()
     A2.close()
+
+
+@pytest.mark.parametrize("kc", [1, 2, 3, 5])
+@pytest.mark.parametrize("tma", [True, False])
+def test_forced_z_chunks(pkg, oracle, monkeypatch, kc, tma):
+    """Every z-chunk length gives the oracle's A x, in both kernels (TMA and
+    plain loads), on a grid of several x-y tiles so that interior CTAs start
+    at planes 1, 2, … and must zero the z = 0 wall's pinned E themselves."""
+    g = oracle.uniform_grid((64, 48, 13))
+    objs = [oracle.Sphere((30.2, 22.1, 6.3), 5.1, 12.25)]
+    S = oracle.System(g, 2 * np.pi / 12, ((4, 4, 3), (4, 4, 3)), objs)
+    monkeypatch.setenv("FDFD_KCHUNK", str(kc))
+    monkeypatch.setenv("FDFD_DISABLE_TMA", "0" if tma else "1")
+    A = _make_op(pkg, S)
+    x = _rand(A.n, 29)
+    ref = S.A @ x
+    assert np.linalg.norm(A.matvec(x, "c128") - ref) / np.linalg.norm(ref) <= TOL64
+    assert np.linalg.norm(A.matvec(x, "c64") - ref) / np.linalg.norm(ref) <= TOL32
+    A.close()

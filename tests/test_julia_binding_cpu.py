@@ -73,3 +73,22 @@ def test_called_symbols_are_declared(texts):
     assert called
     declared = set(re.findall(r"\b(fdfd_\w+)\s*\(", h))
     assert called <= declared, called - declared
+
+
+def test_rrule_for_the_solve(texts):
+    """The binding defines ChainRulesCore reverse rules for the solve with
+    respect to ε (solve_with_eps) and b (A \\ b); their pullbacks run the
+    transposed GPU solve (transpose = 1 in the options they pass)."""
+    _, j = texts
+    assert re.search(r"function ChainRulesCore\.rrule\(::typeof\(solve_with_eps\), A::FDFDOperator", j)
+    assert re.search(r"function ChainRulesCore\.rrule\(::typeof\(\\\), A::FDFDOperator", j)
+    pb = re.search(r"function solve_pullback\(.*?\nend", j, re.S).group(0)
+    assert "opts.use_graph" in pb and ", 1,\n" in pb    # the transpose flag
+    assert "2 .* real.((A.ω^2) .* λ .* e)" in j          # ε̄ = 2Re(ω²λe)
+    assert "2 .* conj.(λ)" in j                            # b̄ = 2 conj(λ)
+
+
+def test_device_residual_wrappers(texts):
+    _, j = texts
+    assert "ccall((:fdfd_residual_dev," in j
+    assert "ccall((:fdfd_residual_dev_noalloc," in j

@@ -53,3 +53,37 @@ def test_noalloc_residual_matches_allocating_entry_point(pkg, oracle):
         r_ref = b - S.A @ x
         assert np.linalg.norm(c - r_ref) / np.linalg.norm(r_ref) <= TOL
     A.close()
+
+
+def test_noalloc_residual_lengthens_short_z_chunks(pkg, monkeypatch):
+    """With the z-chunk forced to one plane, a 128×128×260 grid needs 16640
+    thread blocks, more than the fixed scratch's 16384 partial slots; the
+    call lengthens the chunk until the grid fits and still matches
+    fdfd_residual_dev (which sizes its own buffer), on two calls in a row."""
+    torch = pytest.importorskip("torch")
+    lib = pkg._lib.load()
+    N = (128, 128, 260)
+    monkeypatch.setenv("FDFD_KCHUNK", "1")
+    g = pkg.uniform_grid(N)
+    om = 2 * np.pi / 20
+    mdl = pkg.ModelFull(g)
+    pkg.set_ωpml(mdl, om)
+    pkg.set_Npml(mdl, ((8,) * 3, (8,) * 3))
+    A = pkg.create_A(mdl, om)
+    monkeypatch.delenv("FDFD_KCHUNK")
+    dev = torch.device("cuda", 0)
+    gen = torch.Generator(device=dev).manual_seed(3)
+    for call in range(2):
+        xd = torch.randn(A.n, 2, device=dev, dtype=torch.float64, generator=gen)
+        bd = torch.randn(A.n, 2, device=dev, dtype=torch.float64, generator=gen)
+        r1 = torch.zeros_like(xd)
+        r2 = torch.full_like(xd, float("nan"))
+        n1, n2 = C.c_double(), C.c_double()
+        torch.cuda.synchronize()
+        assert lib.fdfd_residual_dev(A._h, C.c_void_p(xd.data_ptr()), C.c_void_p(bd.data_ptr()),
+                                     C.c_void_p(r1.data_ptr()), C.byref(n1)) == 0
+        assert lib.fdfd_residual_dev_noalloc(A._h, C.c_void_p(xd.data_ptr()), C.c_void_p(bd.data_ptr()),
+                                             C.c_void_p(r2.data_ptr()), C.byref(n2)) == 0
+        assert (torch.linalg.vector_norm(r2 - r1) / torch.linalg.vector_norm(r1)).item() <= TOL
+        assert abs(n2.value - n1.value) / n1.value <= TOL
+    A.close()
