@@ -2,7 +2,7 @@
  * fdfd_gb300.h — C ABI of the GB300 FDFD operator and solver.
  *
  * A drop-in for the hot path of MaxwellFDFD.jl: the sparse operator
- *     A = Cₘ·(Pμ \ Cₑ) − ω²·Pε          (src/model/model.jl:248-250)
+ *     A = Cₘ·(Pμ \ Cₑ) − ω²·Pε          (src/model/model.jl:235-237)
  * that the reference assembles as a SparseMatrixCSC{ComplexF64} and the
  * caller then applies (A*x, mul!(y,A,x)) or solves (A\b).  Here A is never
  * assembled: it is applied matrix-free by sm_103a kernels.
@@ -11,11 +11,11 @@
  *   - complex numbers cross the boundary as interleaved (re, im) doubles
  *     (Julia ComplexF64 memory layout);
  *   - field vectors are component-fastest, DOF index c + 3·(i + Nx·(j + Ny·k))
- *     (order_cmpfirst = true, model.jl:85, 88-94);
+ *     (order_cmpfirst = true, model.jl:72, 75-81);
  *   - the stretched ∆l arrays are the outputs of create_stretched_∆ls
- *     (model.jl:135-152);
+ *     (model.jl:122-139);
  *   - the material tensor is the reference's εarr, an (Nx,Ny,Nz,3,3)
- *     column-major ComplexF64 array (model.jl:64; full.jl:16-70).
+ *     column-major ComplexF64 array (model.jl:51; full.jl:16-70).
  *
  * Every call returns an int status (FDFD_OK = 0); none aborts or traps.
  * fdfd_last_error() returns the message of the last failure on a handle.
@@ -85,7 +85,7 @@ typedef struct {
 } fdfd_desc;
 
 /* Shapes for the on-device assignment + subpixel smoothing of ε
- * (replaces add_obj! + calc_matparams!, model.jl:120-133, full.jl:16-70). */
+ * (replaces add_obj! + calc_matparams!, model.jl:107-120, full.jl:16-70). */
 enum { FDFD_SHAPE_SPHERE = 0, FDFD_SHAPE_BOX = 1, FDFD_SHAPE_CYLZ = 2 };
 typedef struct {
   int32_t kind;     /* FDFD_SHAPE_*                                  */
@@ -127,7 +127,7 @@ typedef struct {
 
 /* ---- lifetime ------------------------------------------------------------
  * fdfd_create replaces create_linsys(EE, ω, create_paramops, create_curls, …)
- * (model.jl:222-233) as the point where the operator comes into being. */
+ * (model.jl:209-220) as the point where the operator comes into being. */
 int fdfd_create(const fdfd_desc *desc, fdfd_handle **out);
 void fdfd_destroy(fdfd_handle *h);
 const char *fdfd_last_error(const fdfd_handle *h);   /* h may be NULL        */
@@ -136,7 +136,7 @@ void *fdfd_stream(fdfd_handle *h);                   /* the handle's cudaStream_
 int fdfd_sync(fdfd_handle *h);
 
 /* ---- material ------------------------------------------------------------
- * Pε of create_paramops (model.jl:154-171).  εarr is the reference's
+ * Pε of create_paramops (model.jl:141-158).  εarr is the reference's
  * (Nx,Ny,Nz,3,3) column-major ComplexF64 array: diagonal entries at the E_w
  * samples, off-diagonal entries at E-voxel corners.  This library requires a
  * real, symmetric tensor (lossless dielectric); other input returns
@@ -165,7 +165,7 @@ int fdfd_get_eps(fdfd_handle *h, double *eps_diag, double *eps_off, uint8_t *sma
 int fdfd_set_field_type(fdfd_handle *h, int32_t ft);
 
 /* ---- operator application --------------------------------------------------
- * y = A x (mul!(y, A, x) on the reference's assembled A, model.jl:238-259).
+ * y = A x (mul!(y, A, x) on the reference's assembled A, model.jl:225-246).
  * Host buffers: 2·3·Ncell doubles (ComplexF64).  precision = FDFD_C64
  * computes in complex64 (x rounded, y widened). */
 int fdfd_matvec(fdfd_handle *h, const double *x, double *y, int32_t precision);
@@ -176,7 +176,7 @@ int fdfd_matvec_dev(fdfd_handle *h, const void *x, void *y, int32_t precision);
 int fdfd_matvec_transpose(fdfd_handle *h, const double *x, double *y, int32_t precision);
 /* r = b − A x and rnorm2 = ‖r‖₂², all complex128 device buffers (double2,
  * 3·Ncell each), computed in FP64 by the operator kernel with a fused
- * reduction (the true residual of create_linsys's system, model.jl:222-233,
+ * reduction (the true residual of create_linsys's system, model.jl:209-220,
  * that a caller checks a solution against).  Returns once rnorm2 is on the
  * host.  Uses the handle's reduction buffer. */
 int fdfd_residual_dev(fdfd_handle *h, const void *x, const void *b, void *r, double *rnorm2);
@@ -245,7 +245,7 @@ int fdfd_corner_mean_dev(fdfd_handle *h, int32_t field, const void *in, void *ou
 
 /* ---- adjoint gradient --------------------------------------------------------
  * No counterpart in the reference, which only assembles A (create_A,
- * model.jl:238-259) and leaves differentiation to its users.  For A e = b and
+ * model.jl:225-246) and leaves differentiation to its users.  For A e = b and
  * a real objective L(e), pass g = ∂L/∂e, the Wirtinger derivative
  * ½(∂L/∂Re e − i·∂L/∂Im e) (so that dL = 2·Re(gᵀ de)); e.g. for
  * L = |Fᴴe|², g = conj(Fᴴe)·conj(F).  The call solves Aᵀ λ = g with

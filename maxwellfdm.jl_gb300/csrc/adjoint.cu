@@ -1,6 +1,6 @@
 // Adjoint sensitivities of the FDFD solution with respect to ε.
 //
-// For A(ε) e = b with A = Cₘ·Cₑ − ω²·Pε (src/model/model.jl:238-259) and a
+// For A(ε) e = b with A = Cₘ·Cₑ − ω²·Pε (src/model/model.jl:225-246) and a
 // real objective L(e), write g = ∂L/∂e for the Wirtinger derivative
 // ½(∂/∂Re e − i ∂/∂Im e), so that dL = 2·Re(gᵀ de).  Since ∂A/∂ε_cc = −ω²
 // at the E_c sample (pinned wall DOFs included: their row is −ω²ε_cc),

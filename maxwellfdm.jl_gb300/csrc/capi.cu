@@ -2,10 +2,10 @@
 //
 // The reference's boundary for this path is the assembled operator and
 // right-hand side returned by create_linsys / create_A / create_b
-// (src/model/model.jl:222-287), consumed by A*x, mul!(y,A,x) and A\b.
+// (src/model/model.jl:209-274), consumed by A*x, mul!(y,A,x) and A\b.
 // Here the host passes the inputs of that assembly — the stretched ∆l of
-// create_stretched_∆ls (:135-152) and the material tensor εarr
-// (:64, full.jl:16-70) — once, and every application or solve runs on the
+// create_stretched_∆ls (:122-139) and the material tensor εarr
+// (:51, full.jl:16-70) — once, and every application or solve runs on the
 // GPU against device-resident data.
 #include <algorithm>
 #include <cmath>

@@ -3,7 +3,7 @@
 // Data layout in HBM (per handle):
 //   field vectors   AoS complex, component fastest: v[c + 3*cell],
 //                   cell = i + Nx*(j + Ny*k)  (the reference's order_cmpfirst
-//                   DOF order, model.jl:85, 88-94) — float2 or double2.
+//                   DOF order, model.jl:72, 75-81) — float2 or double2.
 //   eps diagonal    SoA real: eps[c*Ncell + cell] = ε_cc at the E_c sample.
 //   eps off-diag    SoA real: eoff[p*Ncell + cell], p = xy, yz, zx, at the
 //                   E-voxel corner (primal³ point) of the cell.

@@ -1,5 +1,5 @@
 // Krylov solvers for A x = b (the reference leaves the solve to the user's
-// A\b on the assembled SparseMatrixCSC, src/model/model.jl:222-233).
+// A\b on the assembled SparseMatrixCSC, src/model/model.jl:209-220).
 //
 // Two precisions share one driver:
 //   FDFD_PREC_FP64   plain complex128 iteration (the comparison baseline);

@@ -1,8 +1,8 @@
 // Matrix-free application of the FDFD operator
 //     y = A x,  A = Cₘ·Cₑ − ω²·Pε   (μ = 1)
 // which the reference assembles as a sparse matrix (create_A,
-// src/model/model.jl:238-259) from create_curls (:173-188) and
-// create_paramops (:154-171).
+// src/model/model.jl:225-246) from create_curls (:160-175) and
+// create_paramops (:141-158).
 //
 // Kernel design (sm_103a, HBM-bound):
 //   * a CTA owns a 32×8 (x,y) tile and marches along z over a chunk of

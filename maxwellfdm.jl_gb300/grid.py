@@ -2,8 +2,8 @@
 
 Mirrors the pieces of MaxwellBase that MaxwellFDFD consumes on this path:
 ``Grid(lprim, isbloch)`` (its ``N``, ``L``, ``bounds``, ``l``, ``∆l`` fields,
-as read by ``add_srce!`` at src/model/model.jl:197-204) and
-``create_stretched_∆ls`` (model.jl:135-152).  These are per-axis arrays of
+as read by ``add_srce!`` at src/model/model.jl:184-191) and
+``create_stretched_∆ls`` (model.jl:122-139).  These are per-axis arrays of
 length N — tiny next to the 3D fields — so they stay host-side; the 3D work
 happens in the CUDA library.
 
@@ -92,7 +92,7 @@ def create_stretched_dl(grid, omega_pml, Npml, pml=PMLParam()):
     """(s∆lₑ, s∆lₘ) for boundft = EE: stretched ∆l at the E-voxel corners
     (primal planes) and at the H-voxel corners (dual planes), per axis.
 
-    Mirrors create_stretched_∆ls (src/model/model.jl:135-152) with
+    Mirrors create_stretched_∆ls (src/model/model.jl:122-139) with
     gₑ = PRIM, gₘ = DUAL."""
     sdl_e = tuple(grid.dl[PRIM][w] * sfactor(grid, w, PRIM, omega_pml, Npml, pml) for w in range(3))
     sdl_m = tuple(grid.dl[DUAL][w] * sfactor(grid, w, DUAL, omega_pml, Npml, pml) for w in range(3))

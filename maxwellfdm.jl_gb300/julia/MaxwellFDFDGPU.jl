@@ -1,7 +1,7 @@
 # MaxwellFDFDGPU — ccall binding of libfdfd_gb300 for MaxwellFDFD.jl.
 #
 # A GPU operator type that is a drop-in for the SparseMatrixCSC that
-# MaxwellFDFD.create_A returns (src/model/model.jl:238-259): it implements
+# MaxwellFDFD.create_A returns (src/model/model.jl:225-246): it implements
 # size, eltype, mul!, *, transpose-mul, ldiv!/\ (GPU Krylov solve) and a
 # ChainRulesCore.rrule for the solve with respect to ε and b.  Signatures
 # mirror include/fdfd_gb300.h one for one.

@@ -3,9 +3,9 @@
 The reference's user flow (src/model/model.jl, full.jl):
 
     mdl = ModelFull(grid)                       full.jl:7-13
-    set_ωpml!(mdl, ω); set_Npml!(mdl, Npml)     model.jl:99-102
-    add_obj!(mdl, "Si", shapes...; ε=12.25)     model.jl:120-133
-    add_srce!(mdl, PointSrc(...))               model.jl:197-204
+    set_ωpml!(mdl, ω); set_Npml!(mdl, Npml)     model.jl:86-89
+    add_obj!(mdl, "Si", shapes...; ε=12.25)     model.jl:107-120
+    add_srce!(mdl, PointSrc(...))               model.jl:184-191
     A, b = create_linsys(EE, ω, create_paramops(mdl), create_curls(mdl), create_srcs(mdl))
     e = A \\ b
 
@@ -219,7 +219,7 @@ def vec2field_arr(v, N):
 
 
 def create_A(mdl, ω, device=0, ft=EE):
-    """The GPU operator (create_A, model.jl:238-259) with ε assigned and
+    """The GPU operator (create_A, model.jl:225-246) with ε assigned and
     smoothed on the device: ft = EE → A = Cₘ Cₑ − ω² Pε on E; ft = HH →
     A = Cₑ (Pε \\ Cₘ) − ω² on H (diagonal ε only, as in the reference)."""
     sdl_e, sdl_m = create_stretched_dls(mdl)
@@ -233,7 +233,7 @@ def create_A(mdl, ω, device=0, ft=EE):
 
 
 def create_b(mdl, ω, ft=EE, A=None):
-    """b = −iω jₑ (create_b, model.jl:264-287, jₘ = 0); for a 2D model, the
+    """b = −iω jₑ (create_b, model.jl:251-274, jₘ = 0); for a 2D model, the
     slice's components only (component fastest).  ft = HH: b = Cₑ (Pε \\ jₑ),
     formed on the GPU by the operator A of the same model (its ε and its
     curl), as (−iω)·h_from_e(ε⁻¹ jₑ)."""

@@ -1,7 +1,7 @@
 """GPU FDFD operator: the drop-in for the reference's assembled A.
 
 The reference returns ``A = Cₘ·(Pμ \\ Cₑ) − ω²·Pε`` as a
-``SparseMatrixCSC{ComplexF64}`` (create_A, src/model/model.jl:238-259) and
+``SparseMatrixCSC{ComplexF64}`` (create_A, src/model/model.jl:225-246) and
 the caller applies ``A*x`` / ``mul!(y, A, x)`` or solves ``A\\b``.
 ``FDFDOperator`` exposes the same operations — ``A @ x``, ``A.T @ x``,
 ``A.solve(b)`` — executed matrix-free by libfdfd_gb300 on one GPU.

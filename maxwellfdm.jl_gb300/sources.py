@@ -1,7 +1,7 @@
 """Current sources: the host-side mirror of src/source/*.jl.
 
 ``distweights`` splits a point location over the two nearest grid planes
-(src/source/source.jl:278-376); ``PointSrc`` (pointsrc.jl:51-103) and
+(src/source/source.jl:208-306); ``PointSrc`` (pointsrc.jl:51-103) and
 ``PlaneSrc`` (planesrc.jl:14-80) distribute a dipole or a current sheet onto
 the J array.  These are O(1)/O(plane) host operations; the right-hand side
 b = -iω J then crosses to the GPU with the solve.

@@ -2,7 +2,7 @@
  * CPU baseline and test infrastructure (oracle): complex128 CSR sparse
  * matrix-vector product, unpreconditioned BiCGSTAB and BiCGStab(l)
  * (Sleijpen & Fokkema 1993) on all host cores (OpenMP).  The matrix is the oracle's assembled A = Cm*Ce - w^2*Peps
- * (the reference's create_A, src/model/model.jl:238-259, which Julia then
+ * (the reference's create_A, src/model/model.jl:225-246, which Julia then
  * applies with its single-threaded SparseArrays SpMV and solves with A\b).
  * The recurrence is the one in fdfd_oracle.bicgstab (van der Vorst 1992):
  *   rho = <rh, r>, beta = (rho/rho_old)(alpha/omega), p = r + beta(p - omega v),

@@ -8,17 +8,17 @@ never as the thing measured on the GPU path.
 What it restates (plain numpy/scipy, complex128):
 
 * the Yee grid with ghost points (MaxwellBase ``Grid``, as used at
-  src/model/model.jl:135-152 and test/source.jl:6-15, 350-351);
+  src/model/model.jl:122-139 and test/source.jl:6-15, 130);
 * ``distweights`` and the PointSrc / PlaneSrc current assembly
-  (src/source/source.jl:278-376, src/source/pointsrc.jl:64-103,
+  (src/source/source.jl:208-306, src/source/pointsrc.jl:64-103,
   src/source/planesrc.jl:34-80);
-* stretched-coordinate PML ∆l (``create_stretched_∆ls``, model.jl:135-152);
-* the curl operators Cₑ, Cₘ (``create_curls``, model.jl:173-188);
+* stretched-coordinate PML ∆l (``create_stretched_∆ls``, model.jl:122-139);
+* the curl operators Cₑ, Cₘ (``create_curls``, model.jl:160-175);
 * the ε parameter operator with off-diagonal averaging
-  (``create_paramops``, model.jl:154-171);
+  (``create_paramops``, model.jl:141-158);
 * point-in-object assignment plus Kottke subpixel smoothing with the
   dual-voxel object-index trick (``calc_matparams!``, src/model/full.jl:16-70);
-* ``create_A`` / ``create_b`` / ``h_from_e`` (model.jl:238-292);
+* ``create_A`` / ``create_b`` / ``h_from_e`` (model.jl:225-279);
 * an FP64 BiCGSTAB (the reference has no solver; users call ``A\\b``).
 
 Parity status.  The source discretisation (``distweights``, PointSrc,
@@ -36,7 +36,7 @@ A1  boundft = EE on every axis.  A non-Bloch axis is a PEC wall at both ends:
     kept in the vector but pinned: their Cₑ columns are zero) and at the
     positive-end ghost primal plane.  H ghosts at the negative end mirror
     H at index 0.  This matches the zeroing of primal-plane currents on
-    symmetry boundaries in ``distweights`` (source.jl:313-314).
+    symmetry boundaries in ``distweights`` (source.jl:243-244).
 A2  PML: s(u) = 1 + σ(u)/(iω_pml), σ = σmax·(d/Lpml)^m with d the depth from
     the PML inner face, σmax = -(m+1)·ln R/(2·Lpml), m = 4, R = 1e-8,
     evaluated at each primal / dual sample location; s∆l = ∆l·s.
@@ -58,7 +58,7 @@ A6  Voxels whose corners hold more than two objects: ε̃ = mean of the corner
 A7  Design region: per-cell ε; ε_ww at an E_w edge touching the region is the
     mean of the 4 cells sharing that edge (cells outside the region take the
     object ε at their centre); off-diagonals are 0 at corners touching it.
-A8  b uses ω, not ωpml (model.jl:275-278); callers set ωpml = ω.
+A8  b uses ω, not ωpml (model.jl:262-265); callers set ωpml = ω.
 A9  μ = 1, so Pμ = I.
 """
 from __future__ import annotations
@@ -80,8 +80,8 @@ class Grid:
     """Yee grid from primal plane locations (both domain ends included).
 
     Restates MaxwellBase ``Grid(lprim, isbloch)`` as it is consumed by
-    ``add_srce!`` (model.jl:197-204: ``grid.bounds, grid.l, grid.∆l``) and as
-    the reference test constructs it (test/source.jl:350-351, 365-366).
+    ``add_srce!`` (model.jl:184-191: ``grid.bounds, grid.l, grid.∆l``) and as
+    the reference test constructs it (test/source.jl:130, 145).
 
     * ``l[PRIM][w]``: the N non-ghost primal planes ``lprim[:-1]``;
       the positive-end plane ``lprim[-1]`` is the primal ghost.
@@ -89,7 +89,7 @@ class Grid:
       dual ghost sits at the negative end (periodic image for Bloch, mirror
       image about lprim[0] otherwise).
     * ``dl[PRIM][w][i] = ldual[i] - ldual[i-1]`` (ghost used for i = 0),
-      ``dl[DUAL][w][i] = lprim[i+1] - lprim[i]`` (test/source.jl:235-236).
+      ``dl[DUAL][w][i] = lprim[i+1] - lprim[i]`` (test/source.jl:14-15).
     """
 
     def __init__(self, lprim, isbloch):
@@ -134,9 +134,9 @@ def uniform_grid(N, h=1.0, isbloch=(False, False, False), origin=0.0):
 def distweights(c, gt, bounds, l, dl, isbloch):
     """Split a point at ``c`` over the two nearest planes of ``l``.
 
-    Restates src/source/source.jl:278-376 line for line in meaning; returns
+    Restates src/source/source.jl:208-306 line for line in meaning; returns
     0-based indices ``(ind1, ind2)`` and weights ``(wt1, wt2)`` (1/length).
-    Raises ValueError where the reference throws ArgumentError (:284, :300).
+    Raises ValueError where the reference throws ArgumentError (:214, :230).
     """
     c = float(c)
     l = np.asarray(l, dtype=np.float64)
@@ -148,19 +148,19 @@ def distweights(c, gt, bounds, l, dl, isbloch):
     N = len(l)
     if not (N > 1 or isbloch):
         raise ValueError(f"length(l) = {N} must be > 1 for symmetry boundary.")
-    zeroing_bc = (gt == PRIM) and not isbloch          # source.jl:313
-    indn = 1 if zeroing_bc else 0                       # source.jl:314
-    indp = N - 1                                        # source.jl:315
-    bc_noeff = l[indn] <= c < l[indp]                   # source.jl:320
+    zeroing_bc = (gt == PRIM) and not isbloch          # source.jl:243
+    indn = 1 if zeroing_bc else 0                       # source.jl:244
+    indp = N - 1                                        # source.jl:245
+    bc_noeff = l[indn] <= c < l[indp]                   # source.jl:250
     if bc_noeff:
-        ind1 = int(np.nonzero(l - c <= 0)[0][-1])       # source.jl:322
+        ind1 = int(np.nonzero(l - c <= 0)[0][-1])       # source.jl:252
         ind2 = ind1 + 1
         dc1 = c - l[ind1]
         dlc = l[ind2] - l[ind1]
     else:
-        if c < l[indn]:                                 # source.jl:327-330
+        if c < l[indn]:                                 # source.jl:257-260
             ind1, ind2, bnd = indn, N - 1, b0
-        else:                                           # source.jl:331-334
+        else:                                           # source.jl:261-264
             ind1, ind2, bnd = indp, 0, b1
         dc1 = abs(l[ind1] - c)
         if gt == PRIM:
@@ -169,14 +169,14 @@ def distweights(c, gt, bounds, l, dl, isbloch):
             dlc = (L - abs(l[ind1] - l[ind2])) if isbloch else 2.0 * abs(l[ind1] - bnd)
     r = dc1 / dlc
     wt1 = 1.0 / dl[ind1]
-    if bc_noeff or isbloch or zeroing_bc:               # source.jl:353
+    if bc_noeff or isbloch or zeroing_bc:               # source.jl:283
         wt1 *= 1.0 - r
-    if c == l[ind1] or (not bc_noeff and not isbloch):  # source.jl:359
+    if c == l[ind1] or (not bc_noeff and not isbloch):  # source.jl:289
         ind2 = ind1
         wt2 = 0.0
     else:
         wt2 = 1.0 / dl[ind2]
-        if bc_noeff or isbloch:                         # source.jl:369
+        if bc_noeff or isbloch:                         # source.jl:299
             wt2 *= r
     return (ind1, ind2), (wt1, wt2)
 
@@ -230,7 +230,7 @@ def add_planesrc(j, gt0, grid, n_axis, c, p, Jdn=1.0):
 
 
 # --------------------------------------------------------------------------
-# PML (create_stretched_∆ls, model.jl:135-152)
+# PML (create_stretched_∆ls, model.jl:122-139)
 # --------------------------------------------------------------------------
 def pml_sfactors(grid, omega_pml, Npml, m=4.0, R=1e-8):
     """s-factors at the N primal and N dual locations of each axis."""
@@ -269,7 +269,7 @@ def stretched_dl(grid, omega_pml, Npml, m=4.0, R=1e-8):
 
 
 # --------------------------------------------------------------------------
-# DOF indexing (component-fastest, order_cmpfirst = true, model.jl:85-94)
+# DOF indexing (component-fastest, order_cmpfirst = true, model.jl:72-81)
 # --------------------------------------------------------------------------
 def field_to_vec(F):
     """(Nx,Ny,Nz,3) field array → vector indexed c + 3(i + Nx(j + Ny k))."""
@@ -368,7 +368,7 @@ def _diff(coo, grid, cout, cin, v, coef, sign, fwd, ph):
 
 def create_curls(grid, sdl_e, sdl_m, kbloch=(0.0, 0.0, 0.0)):
     """Cₑ (E→H, forward differences / s∆lₘ) and Cₘ (H→E, backward
-    differences / s∆lₑ); create_curls, model.jl:173-188."""
+    differences / s∆lₑ); create_curls, model.jl:160-175."""
     n = 3 * grid.ncell
     ph = _bloch_phase(grid, kbloch)
     ce = _Coo(n)
@@ -398,7 +398,7 @@ def create_paramop(grid, eps_diag, eps_off, sdl_e, sdl_m, kbloch=(0.0, 0.0, 0.0)
 
     eps_diag: (Nx,Ny,Nz,3) real/complex, ε_ww at the E_w sample of cell (i,j,k).
     eps_off:  (Nx,Ny,Nz,3) or None, ε_xy, ε_yz, ε_zx at corner (i,j,k).
-    Follows create_paramops, model.jl:154-171 (isfwd_in = boundft .!= EE:
+    Follows create_paramops, model.jl:141-158 (isfwd_in = boundft .!= EE:
     backward averaging of the input to the corners)."""
     n = 3 * grid.ncell
     N = grid.N
@@ -453,7 +453,7 @@ def create_paramop(grid, eps_diag, eps_off, sdl_e, sdl_m, kbloch=(0.0, 0.0, 0.0)
 
 
 def create_A(omega, Peps, Ce, Cm):
-    """A = Cₘ·(Pμ \\ Cₑ) - ω²·Pε with Pμ = I (model.jl:248-250, A9)."""
+    """A = Cₘ·(Pμ \\ Cₑ) - ω²·Pε with Pμ = I (model.jl:235-237, A9)."""
     A = Cm @ Ce
     if omega != 0:
         A = A - (omega ** 2) * Peps
@@ -479,7 +479,7 @@ def create_b_hh(omega, eps_diag_vec, Ce, je_vec, jm_vec=None):
 
 
 def create_b(omega, je_vec, jm_vec=None, Cm=None):
-    """b = -Cₘ(Pμ⁻¹ jₘ) - iω jₑ (model.jl:275-278)."""
+    """b = -Cₘ(Pμ⁻¹ jₘ) - iω jₑ (model.jl:262-265)."""
     b = np.zeros_like(je_vec, dtype=np.complex128)
     if jm_vec is not None and Cm is not None:
         b = -(Cm @ jm_vec)
@@ -919,7 +919,7 @@ class System:
 def adjoint_eps_grad(A, omega, e, g):
     """dL/dε_cc at every E_c sample, (3·Ncell,) real, for A e = b and the
     Wirtinger derivative g = ∂L/∂e (dL = 2·Re(gᵀ de)).  A = K − ω²·Pε
-    (create_A, src/model/model.jl:238-259) gives ∂A/∂ε_cc = −ω² on the
+    (create_A, src/model/model.jl:225-246) gives ∂A/∂ε_cc = −ω² on the
     diagonal, hence de/dε_cc = ω²·A⁻¹(e_c u_c) and
     dL/dε_cc = 2·Re(ω²·λ_c·e_c) with Aᵀλ = g.  The reference has no adjoint;
     this restates the derivative of the operator it assembles.  Direct

@@ -2,7 +2,7 @@
 
 The reference has no adjoint, so the oracle's formula dL/dε_cc =
 2·Re(ω²·λ_c·e_c) (Aᵀλ = g) is checked against central finite differences of
-direct solves of the assembled A (create_A, src/model/model.jl:238-259), and
+direct solves of the assembled A (create_A, src/model/model.jl:225-246), and
 the design chain against the exact linear map of the design-region
 assembly (per-cell ε averaged onto the E edges).
 """

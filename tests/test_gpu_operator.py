@@ -1,6 +1,6 @@
 """GPU operator parity: y = A x from libfdfd_gb300 against the oracle's
 assembled sparse A (the reference's create_A composition,
-src/model/model.jl:248-250), on seeded inputs.
+src/model/model.jl:235-237), on seeded inputs.
 
 Tolerances: complex128 path ≤ 1e-12 relative (2-norm over the vector);
 complex64 path ≤ 1e-5 relative.
