@@ -32,8 +32,6 @@ sys.path.insert(0, ROOT)
 
 METRIC = "time to 1e-6 rel. residual, mixed vs FP64 on same GB300; matvec HBM GB/s"
 WORKLOAD = "96^3 dielectric-sphere scatterer: 40 spheres r~U[3,8] eps=12.25, 10-cell PML, lambda=16, x-pol sheet z=15"
-PROFILE_NOTE = os.path.join(ROOT, "profiles", "solve_96cube_spheres.md")
-NCU_NOTE = os.path.join(ROOT, "profiles", "stencil_c64_96cube.md")
 METHOD, ELL = "bicgstabl", 4   # BiCGStab(4) in both precisions
 
 
@@ -118,31 +116,6 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def _recorded_fp64_matvecs():
-    """Operator applications of the FP64 BiCGStab(4) solve of this workload,
-    recorded from a GPU run in profiles/ (the CPU baseline runs the same
-    recurrence, so it needs the same count)."""
-    try:
-        with open(PROFILE_NOTE) as f:
-            for line in f:
-                if line.startswith("fp64_bicgstabl_matvecs:"):
-                    return int(line.split(":")[1])
-    except OSError:
-        pass
-    return None
-
-
-def _recorded_traffic():
-    try:
-        with open(NCU_NOTE) as f:
-            for line in f:
-                if line.startswith("traffic_bytes_per_launch:"):
-                    return float(line.split(":")[1])
-    except OSError:
-        pass
-    return None
-
-
 _CPU = {}
 
 
@@ -198,34 +171,48 @@ def cpu_sample(seconds=8.0):
     return {"t_mv": t_mv, "matvecs": mv, "t_assemble": c["t_asm"], "nnz": M.nnz, "threads": M.threads}
 
 
+def cpu_full_solve():
+    """One complete FP64 BiCGStab(4) solve of the workload to a relative
+    residual of 1e-6 by the CPU baseline (OpenMP complex128 CSR on all host
+    threads), timed by the wall clock; returns (seconds, applications, true
+    relative residual)."""
+    c = _cpu_system()
+    M, b = c["M"], c["b"]
+    t0 = time.perf_counter()
+    x, mv, _ = M.bicgstabl(b, ell=4, tol=1e-6, maxmv=2000000)
+    t = time.perf_counter() - t0
+    rel = float(np.linalg.norm(b - M.matvec(x)) / np.linalg.norm(b))
+    return t, mv, rel
+
+
 def run_reference(args):
+    """The CPU arm: W + K bounded samples (about 2 s each) of the CPU
+    baseline's per-application time, then ONE complete solve of the same
+    system to 1e-6 timed by the wall clock — the reported value (a full solve
+    takes several minutes on the host cores, so it is not repeated K times)."""
     ws, rank, local = _dist()
     if rank != 0:
-        return 0
-    n_mv = _recorded_fp64_matvecs()
-    if n_mv is None:
-        print(json.dumps({"impl": "reference", "unavailable": "no recorded FP64 operator count to project the "
-                                                              "CPU sample onto (profiles/ note missing)"}))
         return 0
     samples = []
     r = None
     for s in range(args.warmup + args.steps):
-        r = cpu_sample(seconds=6.0)
+        r = cpu_sample(seconds=2.0)
         if s >= args.warmup:
             samples.append(r["t_mv"])
     t_mv = statistics.median(samples)
-    value = t_mv * n_mv
-    sample = (f"{args.steps} samples of {r['matvecs']} operator applications of FP64 BiCGStab(4) (complex128 CSR, "
-              f"{r['nnz']} nnz, OpenMP on {r['threads']} host threads of {os.cpu_count()} ({_cpu_model()}), "
-              f"oracle/csr_bicgstab.c) on the same 96^3 "
-              f"system; median {t_mv*1e3:.2f} ms per application projected to {n_mv} applications (the FP64 "
-              f"BiCGStab(4) count to 1e-6 for this system)")
-    line = {"metric": METRIC, "value": value, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": t_mv * r["matvecs"] * 1e3, "higher_is_better": False,
+    t_full, mv_full, rel_full = cpu_full_solve()
+    sample = (f"one complete FP64 BiCGStab(4) solve to 1e-6 ({mv_full} operator applications, true relres "
+              f"{rel_full:.2e}) of the same 96^3 system by the CPU baseline (complex128 CSR, {r['nnz']} nnz, OpenMP "
+              f"on {r['threads']} host threads of {os.cpu_count()}, {_cpu_model()}; oracle/csr_bicgstab.c), wall "
+              f"clock; plus {args.steps} bounded samples of {r['matvecs']} applications: median "
+              f"{t_mv*1e3:.2f} ms per application")
+    line = {"metric": METRIC, "value": t_full, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_full * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded)", "impl": "reference",
-            "config": {"workload": WORKLOAD, "precision": "fp64", "solver": "BiCGStab(4)"},
-            "cpu_baseline": {"value": value, "unit": "s", "cores": r["threads"], "kind": "port", "sample": sample},
-            "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "config": {"workload": WORKLOAD, "precision": "fp64", "solver": "BiCGStab(4)", "tol": 1e-6},
+            "cpu_baseline": {"value": t_full, "unit": "s", "cores": r["threads"], "kind": "port", "sample": sample},
+            "e2e": {"value": t_full, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "cpu_matvecs": mv_full, "cpu_relres": rel_full, "cpu_ms_per_application": t_mv * 1e3}
     print(json.dumps(line))
     return 0
 
@@ -280,7 +267,15 @@ def run_ours(args):
     ev1.synchronize()
     t_fp64 = max_over_ranks(ev0.elapsed_time(ev1) / 1e3, ws, dev)
     x_fp64 = x64_dev.cpu().numpy().view(np.complex128).reshape(-1)
-    ferr = float(np.linalg.norm(x_mixed - x_fp64) / np.linalg.norm(x_fp64))
+    # field error against an accurate FP64 solution (continued from the FP64
+    # solve to a 1e-9 residual; untimed): at 1e-6 both solves still carry
+    # errors of that order times the conditioning, so they are not compared
+    # with each other
+    A.solve_dev(b_dev.data_ptr(), x64_dev.data_ptr(), tol=1e-9, precision="fp64", method=METHOD, ell=ELL,
+                x0_given=True)
+    x_ref = x64_dev.cpu().numpy().view(np.complex128).reshape(-1)
+    ferr = float(np.linalg.norm(x_mixed - x_ref) / np.linalg.norm(x_ref))
+    ferr64 = float(np.linalg.norm(x_fp64 - x_ref) / np.linalg.norm(x_ref))
 
     # operator kernel roofline: complex64 A·x launches on inputs > L2, L2 flushed before each
     ed, eo, _ = A.get_eps()
@@ -356,14 +351,14 @@ def run_ours(args):
             "iterations": stats[-1]["iterations"], "fp64_iterations": st64["iterations"],
             "matvecs": stats[-1]["matvecs"], "fp64_matvecs": st64["matvecs"],
             "refinements": stats[-1]["refinements"], "relres": stats[-1]["relres"],
-            "fp64_relres": st64["relres"], "field_err_vs_fp64": ferr,
+            "fp64_relres": st64["relres"], "field_err_vs_fp64_1e-9": ferr, "fp64_field_err_vs_fp64_1e-9": ferr64,
             "matvec_c64_us": t_mv * 1e6, "matvec_c128_us": t_mv128 * 1e6,
             "cells_per_s_c64": A.ncell / t_mv,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": achieved / hbm_peak, "traffic": _recorded_traffic(),
+                         "frac": achieved / hbm_peak, "traffic": None,
                          "kernel": "k_apply_tma<float, EPI_STORE> (y = A x, complex64)",
                          "alg_bytes_per_launch": alg64,
-                         "traffic_source": "profiles/stencil_c64_96cube.md (ncu, same workload, one launch)",
+                         "traffic_note": "ncu dram bytes per launch are kept in profiles/, not read by this script",
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s"},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 16 * n},
