@@ -389,7 +389,13 @@ def run_profile(args):
         pkg.set_ωpml(mdl, om)
         pkg.set_Npml(mdl, ((10,) * 3, (10,) * 3))
         rng = np.random.default_rng(7)
-        for c, r, e in pkg.workloads._spheres(rng, N, 10, 40, 3.0, 8.0, [12.25]):
+        if args.spheres == "c5":
+            # the 320³ workload's sphere statistics, count scaled to the grid volume
+            nsph = max(1, int(round(400 * np.prod(N) / 320 ** 3)))
+            sph = pkg.workloads._spheres(rng, N, 12, nsph, 4.0, 16.0, [1.0, 2.25, 12.25])
+        else:
+            sph = pkg.workloads._spheres(rng, N, 10, 40, 3.0, 8.0, [12.25])
+        for c, r, e in sph:
             pkg.add_obj(mdl, "dielectric", pkg.Sphere(c, r), ε=e)
         A = pkg.create_A(mdl, om)
         prec = args.precision
@@ -427,6 +433,8 @@ def main():
     ap.add_argument("--grid", default="256,256,128")
     ap.add_argument("--precision", default="c64", choices=["c64", "c128"])
     ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--spheres", default="c2", choices=["c2", "c5"],
+                    help="profile matvec: sphere statistics of the 96^3 (c2) or the 320^3 (c5) workload")
     ap.add_argument("--maxit", type=int, default=100)
     args = ap.parse_args()
     if args.profile:
