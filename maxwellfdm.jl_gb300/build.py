@@ -17,7 +17,7 @@ LIB = os.path.join(HERE, "libfdfd_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-Xptxas", "-O3"]
-SOURCES = ["stencil.cu", "blas1.cu", "solver.cu", "capi.cu", "setup.cu", "noalloc.cu", "adjoint.cu", "fields.cu", "hh.cu", "bicgl.cu"]
+SOURCES = ["stencil.cu", "stencil2.cu", "blas1.cu", "solver.cu", "capi.cu", "setup.cu", "noalloc.cu", "adjoint.cu", "fields.cu", "hh.cu", "bicgl.cu"]
 # setup.cu must round exactly like the CPU oracle (bit-identical object
 # indices and smoothing masks): no fused multiply-add contraction there.
 PER_SOURCE = {"setup.cu": ["--fmad=false"]}

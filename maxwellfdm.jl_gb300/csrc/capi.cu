@@ -449,6 +449,8 @@ int fdfd_create(const fdfd_desc *d, fdfd_handle **out) {
     h->pdl = pd != nullptr && pd[0] != '\0' && pd[0] != '0';
     const char *kc = std::getenv("FDFD_KCHUNK");
     if (kc != nullptr) h->kc_force = std::max(1, std::min(std::atoi(kc), h->N[2]));
+    const char *ov = std::getenv("FDFD_OPERATOR_V2");
+    if (ov != nullptr) h->op_variant = std::atoi(ov);
     const char *wl = std::getenv("FDFD_WAIT_LIMIT_CLOCKS");
     if (wl != nullptr) h->wait_limit = std::max(0ll, std::min(std::atoll(wl), h->wait_limit));
   }
@@ -713,6 +715,7 @@ static fdfd_handle *make_worker(fdfd_handle *p, int *rc) {
   w->kc[1] = p->kc[1];
   w->kc_force = p->kc_force;
   w->wait_limit = p->wait_limit;
+  w->op_variant = p->op_variant;
   w->tuned_off = p->tuned_off;
   w->shares_operator = true;
   *rc = FDFD_OK;

@@ -161,6 +161,13 @@ struct fdfd_handle {
   // gives up (≈1 s); FDFD_WAIT_LIMIT_CLOCKS lowers it, so that a test can
   // make a wait run out and see FDFD_ERR_TIMEOUT without hanging anything
   long long wait_limit = 1ll << 31;
+  // layout of the second TMA operator kernel (stencil2.cu), from
+  // FDFD_OPERATOR_V2 at create: 0 = first TMA kernel only; 4 (default) = two
+  // rows per warp, 4-slot ring, ε diagonal from global memory, 2 CTAs per SM;
+  // 1 = one row per warp, 4 slots, 3 CTAs; 2 = two rows, 3 slots, ε diagonal
+  // through the ring; 3 = as 1 with 2 CTAs.  Measured at 320³ with 400
+  // spheres: 4: 439 µs, 2: 496 µs, 3: 494 µs, 1: 556 µs, first kernel 525 µs.
+  int op_variant = 4;
   int tuned_off = -1;                 // has_off at the last tuning (−1: not tuned yet)
   std::string err;
 };
@@ -189,6 +196,11 @@ template <typename R> OpArgs<R> op_args(const fdfd_handle *h);
 template <typename R>
 int launch_apply_fin(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R>::C *y, int epi,
                      const typename CT<R>::C *aux0, int fin, KScalars *sc, bool transpose);
+// the second TMA operator kernel (stencil2.cu); FDFD_ERR_UNSUPPORTED when it
+// does not serve the call (the caller then uses the first one)
+template <typename R>
+int launch_apply_v2(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R>::C *y, int epi,
+                    const typename CT<R>::C *aux0, int fin, KScalars *sc, int kc);
 // number of blocks launch_apply uses (reduction buffer sizing)
 int apply_blocks(const fdfd_handle *h);
 // pick the z-chunk length per precision by timing (stencil.cu)

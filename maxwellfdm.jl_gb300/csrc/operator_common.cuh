@@ -7,6 +7,8 @@
 
 namespace fdfd {
 
+constexpr int KCMAX = 64;  // longest z-chunk of the operator kernels (the autotuner's range)
+
 template <typename R>
 struct Extra {
   using C = typename CT<R>::C;
@@ -15,6 +17,7 @@ struct Extra {
   C ph[3], phinv[3];  // Bloch e^{-ikL} and its inverse
   int kchunk;
   int eoff_tma;       // TMA kernel: off-diagonal ε staged through the shared-memory ring
+  int ediag_tma;      // second TMA kernel: ε diagonal staged through the ring
   long long wait_limit;  // TMA kernel: SM clocks a pipeline wait may take before it gives up
 };
 
@@ -27,6 +30,13 @@ __device__ __forceinline__ typename CT<R>::C vol_e(const Extra<R> &ex, int c, in
   v = cmul(v, (c == 1) ? ex.sdlm[1][g[1]] : ex.sdle[1][g[1]]);
   v = cmul(v, (c == 2) ? ex.sdlm[2][g[2]] : ex.sdle[2][g[2]]);
   return v;
+}
+
+// c·v for a coefficient c that is real when RC (tiles outside the PML)
+template <bool RC, typename C>
+__device__ __forceinline__ C mulc(C c, C v) {
+  if constexpr (RC) return cscale(v, c.x);
+  else return cmul(c, v);
 }
 
 template <typename C>

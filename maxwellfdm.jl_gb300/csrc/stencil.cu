@@ -33,6 +33,7 @@
 
 #include "krylov_fin.cuh"
 #include "operator_common.cuh"
+#include "tma_util.cuh"
 
 namespace fdfd {
 
@@ -100,7 +101,6 @@ struct PlainSmem {
 // Per-chunk copies of the z coefficient arrays and the off-diagonal flags of
 // the tile column, indexed by plane − (k0 − 1) over k0 − 1 … k1 (staged once
 // per CTA, so no plane waits on a global load for them).
-constexpr int KCMAX = 64;  // longest z-chunk (the autotuner's range)
 template <typename R>
 struct ZTile {
   using C = typename CT<R>::C;
@@ -179,12 +179,6 @@ __device__ __forceinline__ void fill_coef(CoefTile<R> &T, const OpArgs<R> &a, in
 
 // H = Cₑ E at tile position (ii, jj) of plane k (E(k), E(k+1) in slots sk,
 // sk1); also returns E(k) there.
-// c·v for a coefficient c that is real when RC (tiles outside the PML)
-template <bool RC, typename C>
-__device__ __forceinline__ C mulc(C c, C v) {
-  if constexpr (RC) return cscale(v, c.x);
-  else return cmul(c, v);
-}
 
 template <typename R, bool RC, typename ET>
 __device__ __forceinline__ void curl_e(const ET &E, const CoefTile<R> &T, typename CT<R>::C cmz, int sk, int sk1,
@@ -528,57 +522,6 @@ __global__ void __launch_bounds__(NTHR, sizeof(R) == 4 ? 3 : 2) k_apply(OpArgs<R
 }
 
 // ------------------------------------------------------------------ TMA kernel
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void tma_copy3d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2,
-                                           uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-      "[%5];" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
-      : "memory");
-}
-__device__ __forceinline__ void tma_copy4d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
-                                           uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
-      "[%6];" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
-      : "memory");
-}
-// Bounded wait on an mbarrier phase: gives up after `limit` SM clocks
-// (WAIT_LIMIT ≈ 2^31, about one second) and reports false instead of
-// spinning forever.  limit = 0 tests the phase once without waiting.
-constexpr long long WAIT_LIMIT = 1ll << 31;
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long long limit = WAIT_LIMIT) {
-  if (limit <= 0) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-        : "=r"(done)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return done != 0;
-  }
-  const long long t0 = clock64();
-  while (true) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-        : "=r"(done)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (done) return true;
-    if (clock64() - t0 > limit) return false;
-  }
-}
-
 // Zero the pinned DOFs of a freshly landed plane (their Cₑ columns are 0):
 // E_y, E_z on x = 0; E_x, E_z on y = 0; E_x, E_y on z = 0 (PEC walls).
 // Run by the warp that waited for the plane (lane, 32 lanes), so the block
@@ -866,6 +809,7 @@ Extra<R> make_extra(const fdfd_handle *h) {
   Extra<R> ex;
   ex.kchunk = kchunk_for(h, sizeof(R) == 4);
   ex.eoff_tma = 0;
+  ex.ediag_tma = 0;
   ex.wait_limit = h->wait_limit;
   const C *coef;
   if constexpr (sizeof(R) == 8) coef = reinterpret_cast<const C *>(h->coef64);
@@ -896,6 +840,7 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   }();
   return fn;
 }
+PFN_cuTensorMapEncodeTiled_v12000 tensor_encode_fn() { return encode_fn(); }
 
 // The TMA kernel serves PEC (non-Bloch) walls, the forward operator, 16-byte
 // aligned inputs and an x row pitch that is a multiple of 16 bytes.
@@ -955,6 +900,10 @@ static int launch_t(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R>::
     if (rc) return rc;
   }
   const int d = h->dev;
+  if (!TR && EPI != EPI_DOT_SU && tma_ok<R>(h, x, TR)) {
+    const int rc2 = launch_apply_v2<R>(h, x, y, EPI, aux0, fin, sc, ex.kchunk);
+    if (rc2 != FDFD_ERR_UNSUPPORTED) return rc2;
+  }
   if (!TR && tma_ok<R>(h, x, TR)) {
     static DevFlags attr_tma;
     const int smem = TmaGeom<R>::SMEM;
