@@ -258,9 +258,9 @@ __global__ void __launch_bounds__(V2<R, RW, NS, EDR>::NT, MB)
   const int plane = a.N[0] * a.N[1];  // 3·Ncell < 2³¹ (checked at launch)
   const int nc = (int)a.ncell;
 
-  // The march over the chunk.  WALL: the CTA touches a low PEC wall (i0, j0
-  // or k0 = 0) and may meet pinned DOFs; the other CTAs run without the
-  // pin selects.
+  // The march over the chunk.  WALL: the CTA touches a low PEC wall (i0 or j0
+  // = 0, or planes from k0 − 1 ≤ 0) and may meet pinned DOFs; the other CTAs
+  // run without the pin selects.
   auto march = [&](auto wall_tag) {
     constexpr bool WALL = decltype(wall_tag)::value;
     bool ok = mbar_wait_sleep(smem_u32(&bars[0]), 0, ex.wait_limit, 100000u);
@@ -609,7 +609,8 @@ __global__ void __launch_bounds__(V2<R, RW, NS, EDR>::NT, MB)
       s1 = s1 + 1 == NS ? 0 : s1 + 1;
     }
   };
-  if (i0 == 0 || j0 == 0 || k0 == 0) march(std::true_type{});
+  // a chunk starting at plane 1 reads the z = 0 wall plane as its plane k−1
+  if (i0 == 0 || j0 == 0 || k0 <= 1) march(std::true_type{});
   else march(std::false_type{});
 
   if (!run) {
