@@ -217,6 +217,46 @@ def run_reference(args):
     return 0
 
 
+def operator_320(pkg, dev, hbm_peak, reps=10):
+    """The complex64 and complex128 operator on the 320³ workload (400
+    spheres r ~ U[4, 16], ε ∈ {1, 2.25, 12.25}, 12-cell PML, λ = 24): CUDA
+    events on the library's stream around single launches, L2 flushed by a
+    256 MiB read before each (inputs 0.8 / 1.6 GB, far above L2)."""
+    import torch
+    mdl, om, _ = pkg.workloads.config5()
+    A = pkg.create_A(mdl, om)
+    _, eo, _ = A.get_eps()
+    n_off = int(np.count_nonzero(np.any(eo != 0, axis=-1)))
+    del eo
+    stream = torch.cuda.ExternalStream(A.stream, device=dev)
+    flush = torch.ones(64 << 20, dtype=torch.float32, device=dev)
+    out = {"workload": "320^3, 400 spheres r~U[4,16] eps in {1,2.25,12.25}, 12-cell PML, lambda=24",
+           "cells": A.ncell, "off_diagonal_corners": n_off}
+    for prec, dt, per_cell, per_off in (("c64", torch.float32, 60, 12), ("c128", torch.float64, 120, 24)):
+        xin = torch.randn(A.n, 2, device=dev, dtype=dt)
+        yout = torch.empty_like(xin)
+        ts = []
+        with torch.cuda.stream(stream):
+            for r in range(reps + 2):
+                flush.sum()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                A.matvec_dev(xin.data_ptr(), yout.data_ptr(), prec)
+                e1.record(stream)
+                e1.synchronize()
+                if r >= 2:
+                    ts.append(e0.elapsed_time(e1) / 1e3)
+        t = statistics.mean(ts)
+        alg = A.ncell * per_cell + n_off * per_off
+        out[prec] = {"us": t * 1e6, "alg_bytes": alg, "achieved_gbs": alg / t / 1e9,
+                     "frac": alg / t / 1e9 / hbm_peak, "cells_per_s": A.ncell / t}
+        del xin, yout
+    A.close()
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_ours(args):
     import torch
     ws, rank, local = _dist()
@@ -315,6 +355,12 @@ def run_ours(args):
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     achieved = alg64 / t_mv / 1e9
 
+    # the 320³ operator (400 spheres, the workload the ≥ 0.70-of-HBM target
+    # is stated on): complex64 and complex128 A x launches timed the same way
+    op320 = None
+    if not args.no_320 and rank == 0:
+        op320 = operator_320(pkg, dev, hbm_peak)
+
     # end to end through the C ABI with pinned host buffers (copies inside)
     bh = torch.from_numpy(b.view(np.float64).reshape(n, 2).copy()).pin_memory()
     xh = torch.zeros_like(bh).pin_memory()
@@ -360,6 +406,7 @@ def run_ours(args):
                          "alg_bytes_per_launch": alg64,
                          "traffic_note": "ncu dram bytes per launch are kept in profiles/, not read by this script",
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s"},
+            "operator_320": op320,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 16 * n},
             "clocks": clocks,
@@ -429,6 +476,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-320", action="store_true", help="skip the 320^3 operator timing")
     ap.add_argument("--profile", choices=["matvec", "solve"], help="short run for ncu (no bench line)")
     ap.add_argument("--grid", default="256,256,128")
     ap.add_argument("--precision", default="c64", choices=["c64", "c128"])

@@ -15,6 +15,7 @@
 // `check_every` iterations is one CUDA graph replay with no host sync;
 // kernels become no-ops once a stop condition is reached inside a batch.
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -70,6 +71,7 @@ struct Workspace {
   float2 *f[12] = {nullptr};   // inner vectors: BiCGSTAB 7, COCG 4, BiCGStab(ℓ) 2ℓ+4
   double2 *d[12] = {nullptr};
   double2 *w64 = nullptr, *dj64 = nullptr;  // COCG: S weights and Jacobi factors 1/diag(A)
+  double2 *bt = nullptr, *lt = nullptr;     // transposed solves: V⁻¹ b and V μ
   float2 *w32 = nullptr, *dj32 = nullptr;
   KScalars *sc = nullptr, *scu = nullptr;
   KScalars *host = nullptr;  // pinned mirror
@@ -88,6 +90,8 @@ void free_workspace(fdfd_handle *h) {
     cudaFree(ws->f[i]);
     cudaFree(ws->d[i]);
   }
+  cudaFree(ws->bt);
+  cudaFree(ws->lt);
   cudaFree(ws->w64);
   cudaFree(ws->w32);
   cudaFree(ws->dj64);
@@ -470,9 +474,116 @@ static int solve_impl(fdfd_handle *h, const double2 *b, double2 *x, const fdfd_s
   return FDFD_OK;
 }
 
+// out = in · V_E (inverse: in / V_E) per DOF, V_E(c) = s∆lₘ[c][g_c] Π_{v≠c} s∆lₑ[v][g_v]
+// (the dual volume of the E_c sample; in and out may alias)
+__global__ void k_scale_ve(const double2 *__restrict__ coef, int st, int o0, int o1, int o2, int N0, int N1,
+                           long long ncell, const double2 *in, double2 *out, int inverse) {
+  const int off[3] = {o0, o1, o2};
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < 3 * ncell;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(i % 3);
+    const long long cell = i / 3;
+    const int g[3] = {(int)(cell % N0), (int)((cell / N0) % N1), (int)(cell / ((long long)N0 * N1))};
+    double2 v = make_double2(1.0, 0.0);
+    for (int ax = 0; ax < 3; ++ax) {
+      const double2 f = coef[(ax == c ? 5 : 4) * st + off[ax] + g[ax]];
+      v = make_double2(v.x * f.x - v.y * f.y, v.x * f.y + v.y * f.x);
+    }
+    if (inverse) {
+      const double d = v.x * v.x + v.y * v.y;
+      v = make_double2(v.x / d, -v.y / d);
+    }
+    const double2 a = in[i];
+    out[i] = make_double2(a.x * v.x - a.y * v.y, a.x * v.y + a.y * v.x);
+  }
+}
+
+static int scale_ve(fdfd_handle *h, const double2 *in, double2 *out, bool inverse) {
+  k_scale_ve<<<152 * 8, 256, 0, h->stream>>>(h->coef64, h->coef_stride, (int)h->coef_off[0], (int)h->coef_off[1],
+                                             (int)h->coef_off[2], h->N[0], h->N[1], h->ncell, in, out,
+                                             inverse ? 1 : 0);
+  h->launches++;
+  return cuda_check(h, cudaGetLastError(), "k_scale_ve");
+}
+
+// Aᵀ λ = b through the forward operator: V_E·A is complex symmetric, so
+// Aᵀ = V A V⁻¹ and the system is A μ = V⁻¹ b with λ = V μ.  The forward
+// solve runs on the fastest operator kernel; its tolerance is on the scaled
+// residual, so after each solve the true residual ‖b − Aᵀλ‖ is formed in
+// FP64 with the transposed kernel and the forward tolerance tightened (the
+// next solve starting from the current μ) until that residual meets tol.
+template <typename R>
+static int solve_transposed_fwd(fdfd_handle *h, const double2 *b, double2 *x, const fdfd_solve_opts &o,
+                                fdfd_stats &st) {
+  const int ell = o.method == FDFD_BICGSTABL ? o.ell : 1;
+  TRY(ensure_ws(h, sizeof(R) == 4, o.method, ell));
+  Workspace *ws = h->ws;
+  const long long n = ws->n;
+  TRY(alloc(h, (void **)&ws->bt, n * sizeof(double2), "transposed right-hand side"));
+  TRY(alloc(h, (void **)&ws->lt, n * sizeof(double2), "transposed solution"));
+  TRY(dot<double>(h, b, b, n, ws->scu));
+  KScalars tmp;
+  TRY(read_scalars(h, ws->scu, &tmp));
+  const double bb = tmp.dot1.x;
+  st = fdfd_stats{};
+  if (!std::isfinite(bb)) {
+    st.status = FDFD_ERR_NONFINITE;
+    return set_error(h, FDFD_ERR_NONFINITE, "the right-hand side holds a NaN or Inf");
+  }
+  TRY(scale_ve(h, b, ws->bt, true));
+  if (o.x0_given) TRY(scale_ve(h, x, x, true));
+  fdfd_solve_opts oi = o;
+  oi.transpose = 0;
+  double total_ms = 0.0;
+  int rc = FDFD_OK;
+  double relres = 0.0;
+  for (int attempt = 0; attempt < 8; ++attempt) {
+    fdfd_stats si{};
+    rc = solve_impl<R>(h, ws->bt, x, oi, si);
+    st.iterations += si.iterations;
+    st.matvecs += si.matvecs;
+    st.refinements += si.refinements;
+    st.launches += si.launches;
+    total_ms += si.time_ms;
+    if (rc != FDFD_OK) break;
+    // λ = V μ and its true residual in the transposed system
+    TRY(scale_ve(h, x, ws->lt, false));
+    TRY(launch_apply_fin<double>(h, ws->lt, ws->r64, EPI_RESID, b, FIN_NONE, ws->scu, true));
+    TRY(read_scalars(h, ws->scu, &tmp));
+    st.matvecs += 1;
+    relres = bb > 0.0 ? std::sqrt(tmp.dot0.x / bb) : 0.0;
+    if (!(relres > o.tol)) break;
+    oi.tol = oi.tol * std::max(0.05, 0.5 * o.tol / relres);
+    oi.x0_given = 1;
+  }
+  // x takes λ = V μ (also when the forward solve stopped early)
+  TRY(scale_ve(h, x, x, false));
+  TRY(cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync"));
+  st.time_ms = total_ms;
+  if (rc != FDFD_OK) {
+    st.status = rc;
+    return rc;
+  }
+  st.relres = relres;
+  st.status = relres <= o.tol ? FDFD_OK : FDFD_ERR_NOT_CONVERGED;
+  if (st.status != FDFD_OK)
+    return set_error(h, st.status, "the transposed residual did not reach the tolerance");
+  return FDFD_OK;
+}
+
 int solve_dev_impl(fdfd_handle *h, const double2 *b, double2 *x, const fdfd_solve_opts *o, fdfd_stats *st) {
   fdfd_stats tmp;
   fdfd_stats &s = st ? *st : tmp;
+  // transposed systems run through the forward operator unless
+  // FDFD_TRANSPOSE_KERNEL=1 asks for the transposed operator kernel
+  static const bool tkernel = [] {
+    const char *e = std::getenv("FDFD_TRANSPOSE_KERNEL");
+    return e != nullptr && e[0] == '1';
+  }();
+  if (o->transpose && h->ft == FDFD_EE && o->method != FDFD_COCG && !tkernel) {
+    if (o->precision == FDFD_PREC_MIXED) return solve_transposed_fwd<float>(h, b, x, *o, s);
+    return solve_transposed_fwd<double>(h, b, x, *o, s);
+  }
   if (o->precision == FDFD_PREC_MIXED) return solve_impl<float>(h, b, x, *o, s);
   return solve_impl<double>(h, b, x, *o, s);
 }
