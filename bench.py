@@ -402,7 +402,7 @@ def run_ours(args):
             "cells_per_s_c64": A.ncell / t_mv,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "traffic": None,
-                         "kernel": "k_apply_tma<float, EPI_STORE> (y = A x, complex64)",
+                         "kernel": "k_apply_v2<float, EPI_STORE> (y = A x, complex64)",
                          "alg_bytes_per_launch": alg64,
                          "traffic_note": "ncu dram bytes per launch are kept in profiles/, not read by this script",
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s"},
