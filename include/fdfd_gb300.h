@@ -211,6 +211,20 @@ int fdfd_solve(fdfd_handle *h, const double *b, double *x, int32_t nrhs,
  * reference (which solves right-hand sides one by one). */
 int fdfd_solve_batch(fdfd_handle *h, const double *b, double *x, int32_t nrhs, int32_t nworkers,
                      const fdfd_solve_opts *opts, fdfd_stats *stats);
+/* Several independent systems solved together — e.g. the instances of a
+ * batch of uneven grids, frequencies and sources, one entry per right-hand
+ * side: entry i solves hs[i]'s system (A of its grid, ω and ε) for the
+ * complex128 device buffers b[i] → x[i] (3·Ncell of that handle each).  An
+ * entry gets its own stream and Krylov workspace over the handle's operator
+ * data, so entries may name the same handle.  Every round replays the
+ * captured iteration batch (opts.check_every iterations) of each system
+ * still iterating as one parent CUDA graph of child graphs, which the GPU
+ * runs concurrently — small grids fill the machine together — then each
+ * system does its own refinement and stop tests.  All handles on one
+ * device; opts as for fdfd_solve_dev; stats (NULL or n entries) per entry.
+ * Independent of the reference (which solves systems one by one). */
+int fdfd_solve_multi(fdfd_handle *const *hs, int32_t n, const void *const *b, void *const *x,
+                     const fdfd_solve_opts *opts, fdfd_stats *stats);
 /* Device buffers (double2, 3·Ncell each) on the handle's stream; returns
  * after the solve completes. */
 int fdfd_solve_dev(fdfd_handle *h, const void *b, void *x,

@@ -13,7 +13,7 @@ from .model import (EE, HH, Box, DesignRegion, Disk, ModelFull, ModelTE, ModelTM
                     clear_objs, clear_srcs, create_A, create_b, create_linsys, create_stretched_dls, field_arr2vec,
                     field_arr2vec_2d, set_boundft, set_design, set_kbloch, set_Npml, set_ωpml, uniform_lprim2d,
                     vec2field_arr, vec2field_arr_2d)
-from .operator import FDFDOperator
+from .operator import FDFDOperator, solve_multi
 from . import workloads
 from .sources import PlaneSrc, PointSrc, distweights
 
@@ -21,6 +21,6 @@ __all__ = [
     "FDFDError", "load", "Grid", "PMLParam", "uniform_grid", "create_stretched_dl", "PRIM", "DUAL", "EE", "HH",
     "ModelFull", "Sphere", "Box", "DesignRegion", "add_obj", "add_srce", "clear_objs", "clear_srcs", "create_A",
     "create_b", "create_linsys", "create_stretched_dls", "set_boundft", "set_design", "set_kbloch", "set_Npml",
-    "set_ωpml", "field_arr2vec", "vec2field_arr", "FDFDOperator", "PlaneSrc", "PointSrc", "distweights",
+    "set_ωpml", "field_arr2vec", "vec2field_arr", "FDFDOperator", "solve_multi", "PlaneSrc", "PointSrc", "distweights",
     "ModelTE", "ModelTM", "Disk", "Rect", "uniform_lprim2d", "field_arr2vec_2d", "vec2field_arr_2d",
 ]

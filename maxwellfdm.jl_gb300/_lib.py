@@ -98,6 +98,8 @@ SIGNATURES = {
     "fdfd_e_from_h_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "fdfd_corner_mean": (C.c_int, [C.c_void_p, C.c_int32, _dp, _dp]),
     "fdfd_corner_mean_dev": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
+    "fdfd_solve_multi": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                                  C.POINTER(fdfd_solve_opts), C.c_void_p]),
     "fdfd_design_grad_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
 }
 

@@ -65,6 +65,8 @@ int check_dev_err(fdfd_handle *h) {
 }
 
 int solve_dev_impl(fdfd_handle *h, const double2 *b, double2 *x, const fdfd_solve_opts *o, fdfd_stats *st);
+int solve_multi_impl(fdfd_handle *const *hs, int nsys, const double2 *const *b, double2 *const *x,
+                     const fdfd_solve_opts *o, fdfd_stats *st);
 int demote(fdfd_handle *, float2 *, const double2 *, long long);
 int promote(fdfd_handle *, double2 *, const float2 *, long long);
 
@@ -779,6 +781,43 @@ int fdfd_solve_batch(fdfd_handle *h, const double *b, double *x, int32_t nrhs, i
   if (rc) return rc;
   for (int t = 0; t < nworkers; ++t)
     if (rcs[t]) return set_error(h, rcs[t], msgs[t]);
+  return FDFD_OK;
+}
+
+int fdfd_solve_multi(fdfd_handle *const *hs, int32_t n, const void *const *b, void *const *x,
+                     const fdfd_solve_opts *opts, fdfd_stats *stats) {
+  if (!hs || !b || !x || n < 1) return set_error(nullptr, FDFD_ERR_ARG, "bad argument");
+  for (int i = 0; i < n; ++i) {
+    if (!hs[i] || !b[i] || !x[i]) return set_error(hs[i], FDFD_ERR_ARG, "null entry");
+    if (hs[i]->dev != hs[0]->dev) return set_error(hs[0], FDFD_ERR_UNSUPPORTED, "systems on different devices");
+    const int rc = check_opts(hs[i], opts);
+    if (rc) return rc;
+  }
+  FDFD_SET_DEVICE(hs[0]);
+  for (int i = 0; i < n; ++i) {
+    const int rc = cuda_check(hs[i], cudaStreamSynchronize(hs[i]->stream), "stream sync");
+    if (rc) return rc;
+  }
+  // one worker per entry: its own stream, scalars and Krylov workspace over
+  // the shared operator data (entries may name the same handle)
+  int rc = FDFD_OK;
+  std::vector<fdfd_handle *> ws(n, nullptr);
+  for (int i = 0; i < n && rc == FDFD_OK; ++i) ws[i] = make_worker(hs[i], &rc);
+  std::vector<fdfd_stats> tmp(n);
+  std::string msg;
+  if (rc == FDFD_OK) {
+    rc = solve_multi_impl(ws.data(), n, reinterpret_cast<const double2 *const *>(b),
+                          reinterpret_cast<double2 *const *>(x), opts, stats ? stats : tmp.data());
+    if (rc)
+      for (auto *w : ws)
+        if (w && !w->err.empty()) {
+          msg = w->err;
+          break;
+        }
+  }
+  for (auto *w : ws)
+    if (w) fdfd_destroy(w);
+  if (rc) return set_error(hs[0], rc, msg.empty() ? std::string("multi-system solve failed") : msg);
   return FDFD_OK;
 }
 

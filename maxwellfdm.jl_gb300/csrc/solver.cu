@@ -76,6 +76,7 @@ struct Workspace {
   KScalars *sc = nullptr, *scu = nullptr;
   KScalars *host = nullptr;  // pinned mirror
   cudaGraphExec_t gexec[2][3][2] = {};  // [precision][method][transpose]
+  cudaGraph_t graph[2][3][2] = {};      // the captured batches (child graphs of a multi-system round)
   int gbatch[2][3][2] = {};
   int gell[2][3][2] = {};               // ℓ the BiCGStab(ℓ) graph was captured with
   long long gkern[2][3][2] = {};        // kernels per graph replay
@@ -103,6 +104,10 @@ void free_workspace(fdfd_handle *h) {
     for (auto &b : a)
       for (auto &g : b)
         if (g) cudaGraphExecDestroy(g);
+  for (auto &a : ws->graph)
+    for (auto &b : a)
+      for (auto &g : b)
+        if (g) cudaGraphDestroy(g);
   delete ws;
   h->ws = nullptr;
 }
@@ -115,6 +120,13 @@ void drop_graphs(fdfd_handle *h) {
       for (auto &g : b)
         if (g) {
           cudaGraphExecDestroy(g);
+          g = nullptr;
+        }
+  for (auto &a : ws->graph)
+    for (auto &b : a)
+      for (auto &g : b)
+        if (g) {
+          cudaGraphDestroy(g);
           g = nullptr;
         }
 }
@@ -254,46 +266,75 @@ static int cocg_rho(fdfd_handle *h, Workspace *ws, double2 *rho) {
   return FDFD_OK;
 }
 
+// Capture (once) a batch of `batch` iterations as a CUDA graph on the
+// handle's stream; *gout receives the graph (kept for multi-system rounds)
+// and the instantiated executable is kept too.
 template <typename R>
-static int run_batch(fdfd_handle *h, Workspace *ws, int method, int ell, bool tr, int batch, bool use_graph) {
+static int batch_graph(fdfd_handle *h, Workspace *ws, int method, int ell, bool tr, int batch,
+                       cudaGraphExec_t **geout, cudaGraph_t *gout) {
   const int pi = sizeof(R) == 4 ? 1 : 0;
   const int mi = method == FDFD_COCG ? 1 : method == FDFD_BICGSTABL ? 2 : 0;
   const int ti = tr ? 1 : 0;
-  auto body = [&]() -> int {
-    for (int i = 0; i < batch; ++i) {
-      if (method == FDFD_COCG) TRY(cocg_iter<R>(h, ws, tr));
-      else if (method == FDFD_BICGSTABL) TRY(bl_iter<R>(h, ws, ell, tr));
-      else TRY(bicg_iter<R>(h, ws, tr));
-    }
-    return FDFD_OK;
-  };
   // lazily-sized buffers must exist before any capture (the Gram kernel of
   // BiCGStab(ℓ) keeps up to 16 partials per block)
   TRY(ensure_red(h, std::max(apply_blocks(h), method == FDFD_BICGSTABL ? 8 * 152 * 4 : 0)));
-  if (!use_graph) return body();
   cudaGraphExec_t &ge = ws->gexec[pi][mi][ti];
+  cudaGraph_t &gg = ws->graph[pi][mi][ti];
   if (ge && (ws->gbatch[pi][mi][ti] != batch || ws->gell[pi][mi][ti] != ell)) {
     cudaGraphExecDestroy(ge);
     ge = nullptr;
+    if (gg) cudaGraphDestroy(gg);
+    gg = nullptr;
   }
   if (!ge) {
     cudaGraph_t g;
     TRY(cuda_check(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture"));
     const long long l0 = h->launches;
-    int rc = body();
+    int rc = FDFD_OK;
+    for (int i = 0; i < batch && rc == FDFD_OK; ++i) {
+      if (method == FDFD_COCG) rc = cocg_iter<R>(h, ws, tr);
+      else if (method == FDFD_BICGSTABL) rc = bl_iter<R>(h, ws, ell, tr);
+      else rc = bicg_iter<R>(h, ws, tr);
+    }
     ws->gkern[pi][mi][ti] = h->launches - l0;
     h->launches = l0;
     cudaError_t e = cudaStreamEndCapture(h->stream, &g);
     if (rc) return rc;
     TRY(cuda_check(h, e, "end capture"));
     e = cudaGraphInstantiate(&ge, g, 0);
-    cudaGraphDestroy(g);
+    if (e != cudaSuccess) cudaGraphDestroy(g);
     TRY(cuda_check(h, e, "graph instantiate"));
+    gg = g;
     ws->gbatch[pi][mi][ti] = batch;
     ws->gell[pi][mi][ti] = ell;
   }
-  h->launches += ws->gkern[pi][mi][ti];
-  return cuda_check(h, cudaGraphLaunch(ge, h->stream), "graph launch");
+  if (geout) *geout = &ge;
+  if (gout) *gout = gg;
+  return FDFD_OK;
+}
+
+template <typename R>
+static long long batch_kernels(Workspace *ws, int method, bool tr) {
+  const int pi = sizeof(R) == 4 ? 1 : 0;
+  const int mi = method == FDFD_COCG ? 1 : method == FDFD_BICGSTABL ? 2 : 0;
+  return ws->gkern[pi][mi][tr ? 1 : 0];
+}
+
+template <typename R>
+static int run_batch(fdfd_handle *h, Workspace *ws, int method, int ell, bool tr, int batch, bool use_graph) {
+  if (!use_graph) {
+    TRY(ensure_red(h, std::max(apply_blocks(h), method == FDFD_BICGSTABL ? 8 * 152 * 4 : 0)));
+    for (int i = 0; i < batch; ++i) {
+      if (method == FDFD_COCG) TRY(cocg_iter<R>(h, ws, tr));
+      else if (method == FDFD_BICGSTABL) TRY(bl_iter<R>(h, ws, ell, tr));
+      else TRY(bicg_iter<R>(h, ws, tr));
+    }
+    return FDFD_OK;
+  }
+  cudaGraphExec_t *ge = nullptr;
+  TRY(batch_graph<R>(h, ws, method, ell, tr, batch, &ge, nullptr));
+  h->launches += batch_kernels<R>(ws, method, tr);
+  return cuda_check(h, cudaGraphLaunch(*ge, h->stream), "graph launch");
 }
 
 // (Re)initialise the inner iteration from the FP64 residual r64.
@@ -348,130 +389,267 @@ static int init_inner(fdfd_handle *h, Workspace *ws, int method, int ell, double
   return FDFD_OK;
 }
 
+// One system's solve as a resumable state machine: begin() up to the first
+// batch, after_batch() after each replayed batch of iterations (reliable
+// updates, restarts, stop tests), end() for the result and the stats.  The
+// single-system driver alternates run_batch and after_batch; the
+// multi-system driver replays the batches of every unfinished system as
+// child graphs of one parent graph per round.
 template <typename R>
-static int solve_impl(fdfd_handle *h, const double2 *b, double2 *x, const fdfd_solve_opts &o, fdfd_stats &st) {
-  const bool mixed = sizeof(R) == 4;
-  const bool tr = o.transpose != 0;
-  const int ell = o.method == FDFD_BICGSTABL ? o.ell : 1;
-  TRY(ensure_ws(h, mixed, o.method, ell));
-  Workspace *ws = h->ws;
-  const long long n = ws->n;
-  TRY(cuda_check(h, cudaEventRecord(h->ev0, h->stream), "event"));
-  const long long launches0 = h->launches;
-  if (o.x0_given) TRY(cuda_check(h, cudaMemcpyAsync(ws->x64, x, n * sizeof(double2), cudaMemcpyDeviceToDevice,
-                                                    h->stream), "copy x0"));
-  else TRY(cuda_check(h, cudaMemsetAsync(ws->x64, 0, n * sizeof(double2), h->stream), "memset x64"));
-  // ‖b‖²
-  TRY(dot<double>(h, b, b, n, ws->scu));
-  KScalars tmp;
-  TRY(read_scalars(h, ws->scu, &tmp));
-  const double bb = tmp.dot1.x;
-  st = fdfd_stats{};
-  if (!std::isfinite(bb)) {
-    st.status = FDFD_ERR_NONFINITE;
-    return set_error(h, FDFD_ERR_NONFINITE, "the right-hand side holds a NaN or Inf");
-  }
-  if (!(bb > 0.0)) {
-    TRY(cuda_check(h, cudaMemsetAsync(x, 0, n * sizeof(double2), h->stream), "zero x"));
-    st.status = FDFD_OK;
-    return FDFD_OK;
-  }
-  const double tol2 = o.tol * o.tol * bb;
-  double rr;
-  TRY(true_residual(h, b, tr, &rr));
-  st.matvecs = 1;
-  if (!std::isfinite(rr)) {
-    st.status = FDFD_ERR_NONFINITE;
-    return set_error(h, FDFD_ERR_NONFINITE, "the initial residual holds a NaN or Inf (check x0)");
-  }
-  KScalars &hs = ws->host[0];
-  std::memset(&hs, 0, sizeof(KScalars));
-  hs.bb = bb;
-  // recursive-residual target a little below the true target; mixed also
-  // stops every δ-drop for a reliable update
-  hs.stop2 = tol2 * 0.25;
-  hs.upd2 = mixed ? o.delta * o.delta : 0.0;
-  int status = FDFD_ERR_NOT_CONVERGED;
-  int restarts = 0;
-  long long iters = 0;
-  if (rr <= tol2) {
-    status = FDFD_OK;
-  } else {
+struct Solve {
+  fdfd_handle *h = nullptr;
+  const double2 *b = nullptr;
+  double2 *x = nullptr;
+  fdfd_solve_opts o{};
+  fdfd_stats *st = nullptr;
+  Workspace *ws = nullptr;
+  bool tr = false, done = false;
+  int ell = 1, per = 1, batch = 1, mv_per_it = 2, status = FDFD_ERR_NOT_CONVERGED, restarts = 0;
+  long long n = 0, iters = 0, launches0 = 0;
+  double bb = 0.0, tol2 = 0.0, rr = 0.0;
+
+  int begin(fdfd_handle *h_, const double2 *b_, double2 *x_, const fdfd_solve_opts &o_, fdfd_stats *st_) {
+    h = h_;
+    b = b_;
+    x = x_;
+    o = o_;
+    st = st_;
+    const bool mixed = sizeof(R) == 4;
+    tr = o.transpose != 0;
+    ell = o.method == FDFD_BICGSTABL ? o.ell : 1;
+    TRY(ensure_ws(h, mixed, o.method, ell));
+    ws = h->ws;
+    n = ws->n;
+    TRY(cuda_check(h, cudaEventRecord(h->ev0, h->stream), "event"));
+    launches0 = h->launches;
+    if (o.x0_given) TRY(cuda_check(h, cudaMemcpyAsync(ws->x64, x, n * sizeof(double2), cudaMemcpyDeviceToDevice,
+                                                      h->stream), "copy x0"));
+    else TRY(cuda_check(h, cudaMemsetAsync(ws->x64, 0, n * sizeof(double2), h->stream), "memset x64"));
+    // ‖b‖²
+    TRY(dot<double>(h, b, b, n, ws->scu));
+    KScalars tmp;
+    TRY(read_scalars(h, ws->scu, &tmp));
+    bb = tmp.dot1.x;
+    *st = fdfd_stats{};
+    if (!std::isfinite(bb)) {
+      st->status = FDFD_ERR_NONFINITE;
+      done = true;
+      return set_error(h, FDFD_ERR_NONFINITE, "the right-hand side holds a NaN or Inf");
+    }
+    if (!(bb > 0.0)) {
+      TRY(cuda_check(h, cudaMemsetAsync(x, 0, n * sizeof(double2), h->stream), "zero x"));
+      st->status = FDFD_OK;
+      status = FDFD_OK;
+      done = true;
+      bb = 0.0;
+      return FDFD_OK;
+    }
+    tol2 = o.tol * o.tol * bb;
+    TRY(true_residual(h, b, tr, &rr));
+    st->matvecs = 1;
+    if (!std::isfinite(rr)) {
+      st->status = FDFD_ERR_NONFINITE;
+      done = true;
+      return set_error(h, FDFD_ERR_NONFINITE, "the initial residual holds a NaN or Inf (check x0)");
+    }
+    KScalars &hs = ws->host[0];
+    std::memset(&hs, 0, sizeof(KScalars));
+    hs.bb = bb;
+    // recursive-residual target a little below the true target; mixed also
+    // stops every δ-drop for a reliable update
+    hs.stop2 = tol2 * 0.25;
+    hs.upd2 = mixed ? o.delta * o.delta : 0.0;
+    // a BiCGStab(ℓ) cycle counts as ℓ iterations (2ℓ operator applications)
+    per = o.method == FDFD_BICGSTABL ? ell : 1;
+    batch = std::max(1, (o.check_every > 0 ? o.check_every : 50) / per);
+    mv_per_it = o.method == FDFD_COCG ? 1 : 2;
+    if (rr <= tol2) {
+      status = FDFD_OK;
+      done = true;
+      return FDFD_OK;
+    }
     TRY(init_inner<R>(h, ws, o.method, ell, rr, &hs));
     TRY(write_scalars(h, ws->sc, &hs));
-    // a BiCGStab(ℓ) cycle counts as ℓ iterations (2ℓ operator applications)
-    const int per = o.method == FDFD_BICGSTABL ? ell : 1;
-    const int batch = std::max(1, (o.check_every > 0 ? o.check_every : 50) / per);
-    const int mv_per_it = o.method == FDFD_COCG ? 1 : 2;
-    while (true) {
-      TRY(run_batch<R>(h, ws, o.method, ell, tr, batch, o.use_graph != 0));
-      TRY(read_scalars(h, ws->sc, &hs));
-      iters = hs.iter * per;
-      if (hs.done) {
-        if (hs.reason == 4) { status = FDFD_ERR_NONFINITE; break; }
-        // fold the correction into x64 and recompute the true residual
-        if constexpr (sizeof(R) == 4) TRY(accum(h, ws->x64, vec<R>(ws, 0), n));
-        else TRY(accum64(h, ws->x64, vec<R>(ws, 0), n));
-        TRY(true_residual(h, b, tr, &rr));
-        st.matvecs += 1;
-        st.refinements += 1;
-        if (rr <= tol2) { status = FDFD_OK; break; }
-        if (hs.reason == 3) {
-          if (++restarts > 50) { status = FDFD_ERR_BREAKDOWN; break; }
-          const long long it_keep = hs.iter;
-          TRY(init_inner<R>(h, ws, o.method, ell, rr, &hs));
-          hs.iter = it_keep;
-        } else {
-          // reliable update: replace the recursive residual, keep the Krylov state
-          using C = typename CT<R>::C;
-          C *r = vec<R>(ws, o.method == FDFD_BICGSTABL ? 2 : 1);
-          if constexpr (sizeof(R) == 4) TRY(demote(h, r, ws->r64, n));
-          else TRY(copy<double>(h, r, ws->r64, n));
-          hs.rr = rr;
-          hs.rr_max = rr;
-          hs.done = 0;
-          hs.reason = 0;
-          if (o.method == FDFD_COCG) {
-            // COCG's ρ = rᵀ S D⁻¹ r must describe the replaced residual
-            TRY(cocg_rho<R>(h, ws, &hs.rho));
-          } else if (o.method == FDFD_BICGSTABL) {
-            // ρ₁ = (r̂, r_0) and β of the next cycle for the replaced r_0
-            TRY(write_scalars(h, ws->sc, &hs));
-            TRY(bl_redo<R>(h, r, n, FIN_BL_REDO, ws->sc));
-            TRY(read_scalars(h, ws->sc, &hs));
-          }
-        }
-        TRY(write_scalars(h, ws->sc, &hs));
-      }
-      if (iters >= o.maxit) {
-        // fold what we have and report
-        if constexpr (sizeof(R) == 4) TRY(accum(h, ws->x64, vec<R>(ws, 0), n));
-        else TRY(accum64(h, ws->x64, vec<R>(ws, 0), n));
-        TRY(true_residual(h, b, tr, &rr));
-        st.matvecs += 1;
-        status = rr <= tol2 ? FDFD_OK : FDFD_ERR_NOT_CONVERGED;
-        break;
-      }
-    }
-    st.matvecs += iters * mv_per_it;
+    return FDFD_OK;
   }
-  TRY(cuda_check(h, cudaMemcpyAsync(x, ws->x64, n * sizeof(double2), cudaMemcpyDeviceToDevice, h->stream),
-                 "copy x"));
-  TRY(cuda_check(h, cudaEventRecord(h->ev1, h->stream), "event"));
-  TRY(cuda_check(h, cudaEventSynchronize(h->ev1), "event sync"));
-  TRY(check_dev_err(h));
-  float ms = 0.f;
-  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
-  st.iterations = iters;
-  st.relres = std::sqrt(rr / bb);
-  st.time_ms = ms;
-  st.status = status;
-  st.launches = h->launches - launches0;
-  if (status == FDFD_ERR_NOT_CONVERGED)
-    return set_error(h, status, "solver reached maxit before the tolerance");
-  if (status == FDFD_ERR_BREAKDOWN) return set_error(h, status, "Krylov breakdown persisted after restarts");
-  if (status == FDFD_ERR_NONFINITE) return set_error(h, status, "non-finite value in the iteration");
-  return FDFD_OK;
+
+  int after_batch() {
+    KScalars &hs = ws->host[0];
+    TRY(read_scalars(h, ws->sc, &hs));
+    iters = hs.iter * per;
+    if (hs.done) {
+      if (hs.reason == 4) {
+        status = FDFD_ERR_NONFINITE;
+        done = true;
+        return FDFD_OK;
+      }
+      // fold the correction into x64 and recompute the true residual
+      if constexpr (sizeof(R) == 4) TRY(accum(h, ws->x64, vec<R>(ws, 0), n));
+      else TRY(accum64(h, ws->x64, vec<R>(ws, 0), n));
+      TRY(true_residual(h, b, tr, &rr));
+      st->matvecs += 1;
+      st->refinements += 1;
+      if (rr <= tol2) {
+        status = FDFD_OK;
+        done = true;
+        return FDFD_OK;
+      }
+      if (hs.reason == 3) {
+        if (++restarts > 50) {
+          status = FDFD_ERR_BREAKDOWN;
+          done = true;
+          return FDFD_OK;
+        }
+        const long long it_keep = hs.iter;
+        TRY(init_inner<R>(h, ws, o.method, ell, rr, &hs));
+        hs.iter = it_keep;
+      } else {
+        // reliable update: replace the recursive residual, keep the Krylov state
+        using C = typename CT<R>::C;
+        C *r = vec<R>(ws, o.method == FDFD_BICGSTABL ? 2 : 1);
+        if constexpr (sizeof(R) == 4) TRY(demote(h, r, ws->r64, n));
+        else TRY(copy<double>(h, r, ws->r64, n));
+        hs.rr = rr;
+        hs.rr_max = rr;
+        hs.done = 0;
+        hs.reason = 0;
+        if (o.method == FDFD_COCG) {
+          // COCG's ρ = rᵀ S D⁻¹ r must describe the replaced residual
+          TRY(cocg_rho<R>(h, ws, &hs.rho));
+        } else if (o.method == FDFD_BICGSTABL) {
+          // ρ₁ = (r̂, r_0) and β of the next cycle for the replaced r_0
+          TRY(write_scalars(h, ws->sc, &hs));
+          TRY(bl_redo<R>(h, r, n, FIN_BL_REDO, ws->sc));
+          TRY(read_scalars(h, ws->sc, &hs));
+        }
+      }
+      TRY(write_scalars(h, ws->sc, &hs));
+    }
+    if (iters >= o.maxit) {
+      // fold what we have and report
+      if constexpr (sizeof(R) == 4) TRY(accum(h, ws->x64, vec<R>(ws, 0), n));
+      else TRY(accum64(h, ws->x64, vec<R>(ws, 0), n));
+      TRY(true_residual(h, b, tr, &rr));
+      st->matvecs += 1;
+      status = rr <= tol2 ? FDFD_OK : FDFD_ERR_NOT_CONVERGED;
+      done = true;
+    }
+    return FDFD_OK;
+  }
+
+  int end() {
+    st->matvecs += iters * mv_per_it;
+    if (bb > 0.0)
+      TRY(cuda_check(h, cudaMemcpyAsync(x, ws->x64, n * sizeof(double2), cudaMemcpyDeviceToDevice, h->stream),
+                     "copy x"));
+    TRY(cuda_check(h, cudaEventRecord(h->ev1, h->stream), "event"));
+    TRY(cuda_check(h, cudaEventSynchronize(h->ev1), "event sync"));
+    TRY(check_dev_err(h));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    st->iterations = iters;
+    st->relres = bb > 0.0 ? std::sqrt(rr / bb) : 0.0;
+    st->time_ms = ms;
+    st->status = status;
+    st->launches = h->launches - launches0;
+    if (status == FDFD_ERR_NOT_CONVERGED)
+      return set_error(h, status, "solver reached maxit before the tolerance");
+    if (status == FDFD_ERR_BREAKDOWN) return set_error(h, status, "Krylov breakdown persisted after restarts");
+    if (status == FDFD_ERR_NONFINITE) return set_error(h, status, "non-finite value in the iteration");
+    return FDFD_OK;
+  }
+};
+
+template <typename R>
+static int solve_impl(fdfd_handle *h, const double2 *b, double2 *x, const fdfd_solve_opts &o, fdfd_stats &st) {
+  Solve<R> sv;
+  const int rc = sv.begin(h, b, x, o, &st);
+  if (rc) return rc;
+  while (!sv.done) {
+    TRY(run_batch<R>(h, sv.ws, o.method, sv.ell, sv.tr, sv.batch, o.use_graph != 0));
+    TRY(sv.after_batch());
+  }
+  return sv.end();
+}
+
+// Several systems at once (handles hs[i], each with its own stream and
+// workspace): every round replays, as ONE parent CUDA graph, the captured
+// iteration batch of each system still iterating (child graph nodes, which
+// the GPU runs concurrently), then does each system's host-side step.
+template <typename R>
+static int solve_multi(fdfd_handle *const *hs, int nsys, const double2 *const *b, double2 *const *x,
+                       const fdfd_solve_opts &o, fdfd_stats *st) {
+  std::vector<Solve<R>> sv(nsys);
+  int first_rc = FDFD_OK;
+  for (int i = 0; i < nsys; ++i) {
+    const int rc = sv[i].begin(hs[i], b[i], x[i], o, &st[i]);
+    if (rc) {
+      if (!sv[i].done) return rc;  // a CUDA or allocation failure
+      if (first_rc == FDFD_OK) first_rc = rc;
+    }
+  }
+  fdfd_handle *h0 = hs[0];
+  cudaStream_t master = nullptr;
+  TRY(cuda_check(h0, cudaStreamCreateWithFlags(&master, cudaStreamNonBlocking), "stream"));
+  std::vector<cudaEvent_t> evs(nsys + 1, nullptr);
+  int rc = FDFD_OK;
+  for (auto &e : evs)
+    if (rc == FDFD_OK) rc = cuda_check(h0, cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+  cudaGraphExec_t pexec = nullptr;
+  std::vector<int> prev;
+  while (rc == FDFD_OK) {
+    std::vector<int> act;
+    for (int i = 0; i < nsys; ++i)
+      if (!sv[i].done) act.push_back(i);
+    if (act.empty()) break;
+    if (act != prev || !o.use_graph) {
+      if (pexec) cudaGraphExecDestroy(pexec);
+      pexec = nullptr;
+      cudaGraph_t parent = nullptr;
+      rc = cuda_check(h0, cudaGraphCreate(&parent, 0), "graph create");
+      for (int i : act) {
+        if (rc) break;
+        cudaGraph_t child = nullptr;
+        rc = batch_graph<R>(hs[i], sv[i].ws, o.method, sv[i].ell, sv[i].tr, sv[i].batch, nullptr, &child);
+        cudaGraphNode_t node;
+        if (rc == FDFD_OK) rc = cuda_check(h0, cudaGraphAddChildGraphNode(&node, parent, nullptr, 0, child), "child graph");
+      }
+      if (rc == FDFD_OK) rc = cuda_check(h0, cudaGraphInstantiate(&pexec, parent, 0), "graph instantiate");
+      if (parent) cudaGraphDestroy(parent);
+      prev = act;
+    }
+    if (rc) break;
+    // each system's stream → the master stream → the round → back
+    for (int i : act) {
+      if (rc == FDFD_OK) rc = cuda_check(hs[i], cudaEventRecord(evs[i], hs[i]->stream), "event");
+      if (rc == FDFD_OK) rc = cuda_check(h0, cudaStreamWaitEvent(master, evs[i], 0), "wait event");
+    }
+    if (rc == FDFD_OK) rc = cuda_check(h0, cudaGraphLaunch(pexec, master), "graph launch");
+    if (rc == FDFD_OK) rc = cuda_check(h0, cudaEventRecord(evs[nsys], master), "event");
+    for (int i : act) {
+      if (rc) break;
+      rc = cuda_check(hs[i], cudaStreamWaitEvent(hs[i]->stream, evs[nsys], 0), "wait event");
+      hs[i]->launches += batch_kernels<R>(sv[i].ws, o.method, sv[i].tr);
+      if (rc == FDFD_OK) rc = sv[i].after_batch();
+    }
+  }
+  if (pexec) cudaGraphExecDestroy(pexec);
+  cudaStreamSynchronize(master);
+  for (auto &e : evs)
+    if (e) cudaEventDestroy(e);
+  cudaStreamDestroy(master);
+  if (rc) return rc;
+  for (int i = 0; i < nsys; ++i) {
+    const int r = sv[i].end();
+    if (r && first_rc == FDFD_OK) first_rc = r;
+  }
+  return first_rc;
+}
+
+int solve_multi_impl(fdfd_handle *const *hs, int nsys, const double2 *const *b, double2 *const *x,
+                     const fdfd_solve_opts *o, fdfd_stats *st) {
+  if (o->precision == FDFD_PREC_MIXED) return solve_multi<float>(hs, nsys, b, x, *o, st);
+  return solve_multi<double>(hs, nsys, b, x, *o, st);
 }
 
 // out = in · V_E (inverse: in / V_E) per DOF, V_E(c) = s∆lₘ[c][g_c] Π_{v≠c} s∆lₑ[v][g_v]

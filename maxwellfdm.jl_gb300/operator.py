@@ -292,6 +292,31 @@ class FDFDOperator:
             transpose=int(bool(transpose)), use_graph=int(bool(use_graph)))
 
 
+def solve_multi(entries, tol=1e-6, precision="mixed", method="bicgstabl", maxit=200000, delta=0.1,
+                check_every=50, use_graph=True, ell=4):
+    """Solve several independent systems together (fdfd_solve_multi):
+    ``entries`` is a list of (FDFDOperator, b_ptr, x_ptr) with complex128
+    device buffers; entries may share an operator (one per right-hand side).
+    Each round replays every unfinished system's iteration batch as one
+    parent CUDA graph.  Returns the per-entry stats."""
+    if not entries:
+        return []
+    lib = _lib.load()
+    n = len(entries)
+    hs = (C.c_void_p * n)(*[e[0]._h.value for e in entries])
+    bs = (C.c_void_p * n)(*[int(e[1]) for e in entries])
+    xs = (C.c_void_p * n)(*[int(e[2]) for e in entries])
+    o = entries[0][0]._opts(tol, precision, method, maxit, False, delta, check_every, False, use_graph, ell)
+    st = (_lib.fdfd_stats * n)()
+    rc = lib.fdfd_solve_multi(hs, n, bs, xs, C.byref(o), C.cast(st, C.c_void_p))
+    stats = [s.as_dict() for s in st]
+    if rc != _lib.FDFD_OK:
+        err = _lib.FDFDError(rc, (lib.fdfd_last_error(entries[0][0]._h) or b"").decode())
+        err.stats = stats
+        raise err
+    return stats
+
+
 class _Transposed:
     def __init__(self, A):
         self.A = A

@@ -2,9 +2,10 @@
 that do not depend on size.
 
 * Uneven batch (24 instances, edges 48–128, 8-cell PML, 10–60 spheres,
-  1–4 dipoles): three 48³ instances solved concurrently, one handle and one
-  host thread each; every right-hand side meets 1e-6 on the FP64 residual
-  recomputed by the GPU, and for one instance on the oracle's own assembled
+  1–4 dipoles): the whole batch in one fdfd_solve_multi call; and three 48³
+  instances solved concurrently from separate host threads, one handle
+  each.  Every right-hand side meets 1e-6 on the FP64 residual recomputed by
+  the GPU, and one instance per grid size on the oracle's assembled
   matrix.
 * 320³ with 400 spheres (ε ∈ {1, 2.25, 12.25}): on-device smoothing, then
   complex64 against complex128 application, the transpose identity
@@ -134,3 +135,46 @@ def test_batch_of_rhs_on_concurrent_streams(pkg, oracle):
         assert rel <= 1.01e-7, (q, rel)
         assert np.linalg.norm(xb[q] - xs[q]) / np.linalg.norm(xs[q]) < 1e-5
     A.close()
+
+
+def test_config3_all_instances_in_one_multi_solve(pkg, oracle):
+    """The whole uneven batch — all 24 instances (edges 48–128, 10–60
+    spheres, λ ~ U[12, 24]) with each of their 1–4 dipole right-hand sides —
+    in one fdfd_solve_multi call (one parent CUDA graph per round).  Every
+    entry meets 1e-6 on its FP64 residual recomputed by the GPU, and one
+    instance of every grid size meets it on the oracle's assembled matrix."""
+    import torch
+    wl = pkg.workloads
+    dev = torch.device("cuda", 0)
+    ops, entries, bufs = [], [], []
+    for q in range(24):
+        mdl, om, rhs = wl.config3_instance(q)
+        A = pkg.create_A(mdl, om)
+        ops.append((A, mdl, om))
+        for c, p in rhs:
+            b = wl.dipole_rhs(mdl, om, c, p)
+            bd = torch.from_numpy(b.view(np.float64).reshape(-1, 2)).to(dev)
+            xd = torch.zeros_like(bd)
+            entries.append((A, bd.data_ptr(), xd.data_ptr()))
+            bufs.append((q, b, bd, xd))
+    assert len(entries) >= 24
+    stats = pkg.solve_multi(entries, tol=1e-6, precision="mixed")
+    seen = {}
+    for (q, b, bd, xd), st in zip(bufs, stats):
+        assert st["status"] == 0 and st["relres"] <= 1e-6, (q, st)
+        A = ops[q][0]
+        r = torch.empty_like(bd)
+        rr = A.residual_dev(xd.data_ptr(), bd.data_ptr(), r.data_ptr())
+        assert rr ** 0.5 / np.linalg.norm(b) <= 1.01e-6, q
+        seen.setdefault(A.N[0], (q, b, xd))
+    O = oracle
+    for n, (q, b, xd) in sorted(seen.items()):
+        A, mdl, om = ops[q]
+        g = O.uniform_grid(mdl.grid.N)
+        objs = [O.Sphere(o.shape.c, o.shape.r, o.eps) for o in mdl.objects]
+        S = O.System(g, om, mdl.Npml, objs)
+        x = xd.cpu().numpy().view(np.complex128).reshape(-1)
+        rel = np.linalg.norm(b - S.A @ x) / np.linalg.norm(b)
+        assert rel <= 1.02e-6, (n, q, rel)
+    for A, _, _ in ops:
+        A.close()
