@@ -161,8 +161,9 @@ struct fdfd_handle {
   // gives up (≈1 s); FDFD_WAIT_LIMIT_CLOCKS lowers it, so that a test can
   // make a wait run out and see FDFD_ERR_TIMEOUT without hanging anything
   long long wait_limit = 1ll << 31;
-  // layout of the second TMA operator kernel (stencil2.cu), from
-  // FDFD_OPERATOR_V2 at create: 0 = first TMA kernel only; 4 (default) = two
+  // layout of the second TMA operator kernel (stencil2.cu): picked by the
+  // autotuner among 4, 1 and 3 for complex64, or fixed by FDFD_OPERATOR_V2
+  // at create: 0 = first TMA kernel only; 4 (default) = two
   // rows per warp, 4-slot ring, ε diagonal from global memory, 2 CTAs per SM;
   // 1 = one row per warp, 4 slots, 3 CTAs; 2 = two rows, 3 slots, ε diagonal
   // through the ring; 3 = as 1 with 2 CTAs.  Measured at 320³ with 400

@@ -941,7 +941,8 @@ static int launch_t(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R>::
   return cuda_check(h, e, "k_apply launch");
 }
 
-// Autotuner for the z-chunk length: times y = A x for each candidate with
+// Autotuner for the z-chunk length (and, for complex64, the tile layout of
+// the second TMA kernel): times y = A x for each candidate with
 // CUDA events on the handle's stream — one warm-up, then three launches each
 // preceded by an L2 flush (a 192 MiB memset, larger than the 129 MB L2), so
 // the choice holds for inputs streamed from HBM — and keeps the fastest,
@@ -963,43 +964,57 @@ int autotune_kchunk(fdfd_handle *h) {
   int rc = cuda_check(h, cudaMemsetAsync(bx, 0, n * sizeof(double2), h->stream), "memset");
   const int cand[] = {4, 6, 8, 12, 16, 24, 32, 48, 64};
   const bool verbose = std::getenv("FDFD_VERBOSE") != nullptr;
+  // complex64 also picks the tile layout of the second TMA kernel (two rows
+  // per warp with a 4-slot ring; one row per warp with 3 or 2 CTAs per SM)
+  // unless FDFD_OPERATOR_V2 fixed it; complex128 has one layout
+  const bool tune_layout = h->op_variant != 0 && std::getenv("FDFD_OPERATOR_V2") == nullptr;
+  const int layouts_c64[] = {4, 1, 3};
   for (int prec = 0; prec < 2 && rc == FDFD_OK; ++prec) {
     float best = 1e30f;
-    int best_kc = 0, last_chunks = -1;
-    for (int kc : cand) {
-      if (kc > h->N[2] && last_chunks == 1) break;
-      const int chunks = (h->N[2] + kc - 1) / kc;
-      if (chunks == last_chunks) continue;
-      last_chunks = chunks;
-      h->kc[prec] = kc;
-      auto launch = [&]() {
-        return prec == 1 ? launch_apply_fin<float>(h, (const float2 *)bx, (float2 *)by, EPI_STORE, nullptr, FIN_NONE,
-                                                   nullptr, false)
-                         : launch_apply_fin<double>(h, (const double2 *)bx, (double2 *)by, EPI_STORE, nullptr,
-                                                    FIN_NONE, nullptr, false);
-      };
-      if ((rc = launch())) break;
-      float ts[5];
-      for (int r = 0; r < 5 && rc == FDFD_OK; ++r) {
-        cudaMemsetAsync(fl, r, flush_bytes, h->stream);
-        cudaEventRecord(h->ev0, h->stream);
-        rc = launch();
-        cudaEventRecord(h->ev1, h->stream);
-        if (rc || (rc = cuda_check(h, cudaEventSynchronize(h->ev1), "autotune sync"))) break;
-        cudaEventElapsedTime(&ts[r], h->ev0, h->ev1);
-      }
-      if (rc) break;
-      std::sort(ts, ts + 5);
-      const float med = ts[2];
-      if (verbose) fprintf(stderr, "fdfd autotune: %s kchunk %d: %.1f us\n", prec ? "c64" : "c128", kc, med * 1e3);
-      // candidates come in increasing kc (fewer CTAs): take a later one only
-      // if it is clearly faster
-      if (med < 0.97f * best) {
-        best = med;
-        best_kc = kc;
+    int best_kc = 0, best_layout = h->op_variant;
+    const int nlay = (prec == 1 && tune_layout) ? 3 : 1;
+    for (int li = 0; li < nlay && rc == FDFD_OK; ++li) {
+      if (prec == 1 && tune_layout) h->op_variant = layouts_c64[li];
+      int last_chunks = -1;
+      for (int kc : cand) {
+        if (kc > h->N[2] && last_chunks == 1) break;
+        const int chunks = (h->N[2] + kc - 1) / kc;
+        if (chunks == last_chunks) continue;
+        last_chunks = chunks;
+        h->kc[prec] = kc;
+        auto launch = [&]() {
+          return prec == 1 ? launch_apply_fin<float>(h, (const float2 *)bx, (float2 *)by, EPI_STORE, nullptr,
+                                                     FIN_NONE, nullptr, false)
+                           : launch_apply_fin<double>(h, (const double2 *)bx, (double2 *)by, EPI_STORE, nullptr,
+                                                      FIN_NONE, nullptr, false);
+        };
+        if ((rc = launch())) break;
+        float ts[5];
+        for (int r = 0; r < 5 && rc == FDFD_OK; ++r) {
+          cudaMemsetAsync(fl, r, flush_bytes, h->stream);
+          cudaEventRecord(h->ev0, h->stream);
+          rc = launch();
+          cudaEventRecord(h->ev1, h->stream);
+          if (rc || (rc = cuda_check(h, cudaEventSynchronize(h->ev1), "autotune sync"))) break;
+          cudaEventElapsedTime(&ts[r], h->ev0, h->ev1);
+        }
+        if (rc) break;
+        std::sort(ts, ts + 5);
+        const float med = ts[2];
+        if (verbose)
+          fprintf(stderr, "fdfd autotune: %s layout %d kchunk %d: %.1f us\n", prec ? "c64" : "c128", h->op_variant,
+                  kc, med * 1e3);
+        // candidates come in increasing kc (fewer CTAs) and the default
+        // layout first: take a later one only if it is clearly faster
+        if (med < 0.97f * best) {
+          best = med;
+          best_kc = kc;
+          best_layout = h->op_variant;
+        }
       }
     }
     h->kc[prec] = best_kc;
+    if (prec == 1 && tune_layout) h->op_variant = best_layout;
   }
   cudaFree(bx);
   cudaFree(by);
