@@ -158,6 +158,31 @@ __global__ void k_oflags(const double *eoff, long long ncell, int N0, int N1, in
   }
 }
 
+// Flag (x tile, group of g rows, plane k) if any off-diagonal ε that the
+// outputs of those rows at plane k read is non-zero: corners i ∈ [i0, i0+TX],
+// rows j ∈ [g·t, g·t+g], planes k and k+1 (the second TMA kernel's warps own
+// g rows each).
+__global__ void k_oflags_rows(const double *eoff, long long ncell, int N0, int N1, int N2, int tiles_x, int g,
+                              uint8_t *flag) {
+  for (long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x; cell < ncell;
+       cell += (long long)gridDim.x * blockDim.x) {
+    if (eoff[cell] == 0.0 && eoff[ncell + cell] == 0.0 && eoff[2 * ncell + cell] == 0.0) continue;
+    const int i = (int)(cell % N0), j = (int)((cell / N0) % N1), k = (int)(cell / ((long long)N0 * N1));
+    const int tx0 = i / TX, ty0 = j / g;
+    for (int dx = -1; dx <= 0; ++dx) {
+      const int tx = tx0 + dx;
+      if (tx < 0 || (dx == -1 && i % TX != 0)) continue;
+      for (int dy = -1; dy <= 0; ++dy) {
+        const int ty = ty0 + dy;
+        if (ty < 0 || (dy == -1 && j % g != 0)) continue;
+        const long long tc = tx + (long long)tiles_x * ty;
+        flag[tc * N2 + k] = 1;
+        if (k > 0) flag[tc * N2 + k - 1] = 1;
+      }
+    }
+  }
+}
+
 int build_oflags(fdfd_handle *h) {
   if (!h->has_off) return FDFD_OK;
   const int tiles_x = (h->N[0] + TX - 1) / TX, tiles_y = (h->N[1] + TY - 1) / TY;
@@ -171,7 +196,22 @@ int build_oflags(fdfd_handle *h) {
   int rc = cuda_check(h, cudaMemsetAsync(h->oflag, 0, nflag, h->stream), "memset oflag");
   if (rc) return rc;
   k_oflags<<<152 * 4, 256, 0, h->stream>>>(h->eoff64, h->ncell, h->N[0], h->N[1], h->N[2], tiles_x, h->oflag);
-  return cuda_check(h, cudaGetLastError(), "k_oflags");
+  if ((rc = cuda_check(h, cudaGetLastError(), "k_oflags"))) return rc;
+  // per groups of 1 and 2 rows (the second TMA kernel's warp strips)
+  for (int g = 1; g <= 2; ++g) {
+    const size_t nf = (size_t)tiles_x * ((h->N[1] + g - 1) / g) * h->N[2];
+    uint8_t *&f = h->oflag_rows[g - 1];
+    if (!f) {
+      if (dev_malloc(&f, nf) != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(oflag rows) failed");
+      }
+    }
+    if ((rc = cuda_check(h, cudaMemsetAsync(f, 0, nf, h->stream), "memset oflag rows"))) return rc;
+    k_oflags_rows<<<152 * 4, 256, 0, h->stream>>>(h->eoff64, h->ncell, h->N[0], h->N[1], h->N[2], tiles_x, g, f);
+    if ((rc = cuda_check(h, cudaGetLastError(), "k_oflags_rows"))) return rc;
+  }
+  return FDFD_OK;
 }
 
 __global__ void k_to_f32(float *dst, const double *src, long long n) {
@@ -476,6 +516,8 @@ void fdfd_destroy(fdfd_handle *h) {
     cudaFree(h->eoff64);
     cudaFree(h->eoff32);
     cudaFree(h->oflag);
+    cudaFree(h->oflag_rows[0]);
+    cudaFree(h->oflag_rows[1]);
     cudaFree(h->smask);
   }
   cudaFree(h->vx64);
@@ -707,6 +749,8 @@ static fdfd_handle *make_worker(fdfd_handle *p, int *rc) {
   w->eoff64 = p->eoff64;
   w->eoff32 = p->eoff32;
   w->oflag = p->oflag;
+  w->oflag_rows[0] = p->oflag_rows[0];
+  w->oflag_rows[1] = p->oflag_rows[1];
   w->has_off = p->has_off;
   w->smask = p->smask;
   w->slice2d = p->slice2d;

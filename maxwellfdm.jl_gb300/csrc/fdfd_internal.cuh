@@ -134,6 +134,7 @@ struct fdfd_handle {
   double *eoff64 = nullptr;
   float *eoff32 = nullptr;
   uint8_t *oflag = nullptr;
+  uint8_t *oflag_rows[2] = {nullptr, nullptr};  // the same per x tile, group of 1 / 2 rows and plane
   bool has_off = false;
   uint8_t *smask = nullptr;  // 4*ncell smoothing mask (from fdfd_smooth_objects)
   bool has_design = false;   // a design region was applied by fdfd_smooth_objects

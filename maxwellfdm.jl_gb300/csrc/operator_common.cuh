@@ -18,6 +18,7 @@ struct Extra {
   int kchunk;
   int eoff_tma;       // TMA kernel: off-diagonal ε staged through the shared-memory ring
   int ediag_tma;      // second TMA kernel: ε diagonal staged through the ring
+  const uint8_t *oflag_w;  // second TMA kernel: off-diagonal flags per x tile, warp strip and plane
   long long wait_limit;  // TMA kernel: SM clocks a pipeline wait may take before it gives up
 };
 

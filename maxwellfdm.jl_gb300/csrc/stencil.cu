@@ -810,6 +810,7 @@ Extra<R> make_extra(const fdfd_handle *h) {
   ex.kchunk = kchunk_for(h, sizeof(R) == 4);
   ex.eoff_tma = 0;
   ex.ediag_tma = 0;
+  ex.oflag_w = nullptr;
   ex.wait_limit = h->wait_limit;
   const C *coef;
   if constexpr (sizeof(R) == 8) coef = reinterpret_cast<const C *>(h->coef64);

@@ -58,7 +58,6 @@ struct V2 {
   static constexpr int BY = TYT + 2;    // box rows j0−1 … j0+TYT
   static constexpr int PLANE_BYTES = XW * BY * 3 * (int)sizeof(C);
   static constexpr int SLOT = (PLANE_BYTES + 127) / 128 * 128;
-  static constexpr int NSUB = TYT / 8;  // 32×8 off-diagonal flag tiles per CTA tile
   static constexpr int KC2 = KCMAX + 2;
   // exchange, per plane parity: H_x, H_z of the row below each warp ([0]:
   // tile row j0−1, [w+1]: warp w's last row), y-directed corner terms of each
@@ -89,7 +88,7 @@ struct V2 {
   static constexpr int YT_OFF = XT_OFF + 4 * XT_N * (int)sizeof(C);
   static constexpr int ZT_OFF = YT_OFF + 4 * (TYT + 2) * (int)sizeof(C);
   static constexpr int ZF_OFF = ZT_OFF + 4 * KC2 * (int)sizeof(C);
-  static constexpr int BAR_OFF = (ZF_OFF + KC2 * NSUB + 15) / 16 * 16;
+  static constexpr int BAR_OFF = (ZF_OFF + KC2 * NW + 15) / 16 * 16;
   static constexpr int SMEM = BAR_OFF + NS * 8;
   static_assert(SLOT % 128 == 0 && EXCH_OFF % 128 == 0, "TMA destination alignment");
   static_assert(SMEM <= 227 * 1024, "shared memory per CTA");
@@ -143,7 +142,7 @@ __global__ void __launch_bounds__(V2<R, RW, NS, EDR>::NT, MB)
   using G = V2<R, RW, NS, EDR>;
   using C = typename CT<R>::C;
   using X = typename G::Exch;
-  constexpr int NW = G::NW, TYT = G::TYT, KC2 = G::KC2, NSUB = G::NSUB;
+  constexpr int NW = G::NW, TYT = G::TYT, KC2 = G::KC2;
   // indexed directly (not through a realigned generic pointer) so that every
   // access compiles to a shared-memory load with a 32-bit address
   extern __shared__ __align__(128) unsigned char sm[];
@@ -163,7 +162,7 @@ __global__ void __launch_bounds__(V2<R, RW, NS, EDR>::NT, MB)
   const int gi = i0 + lane;
   const int cx = 6 * (i0 - G::XOFF), cy = j0 - 1;
   const int jw = RW * w;  // the warp's first tile row
-  const int tiles_y8 = (a.N[1] + 7) / 8;
+  const int tiles_yr = (a.N[1] + RW - 1) / RW;
   const bool ering = G::EO_SLOT > 0 && ex.eoff_tma != 0;
   const bool edr = G::ED_SLOT > 0 && ex.ediag_tma != 0;
 
@@ -204,13 +203,19 @@ __global__ void __launch_bounds__(V2<R, RW, NS, EDR>::NT, MB)
       zt[KC2 + t] = a.ce[2][c];
       zt[2 * KC2 + t] = a.wm[2][c];
       zt[3 * KC2 + t] = a.wp[2][c];
+      // one flag per warp strip (RW rows): its outputs at plane q read a
+      // non-zero off-diagonal ε (the 32×8 tile flags stand in when the
+      // strip flags are absent)
 #pragma unroll
-      for (int s = 0; s < NSUB; ++s) {
-        const int t8 = j0 / 8 + s;
+      for (int s = 0; s < NW; ++s) {
+        const int tr = j0 / RW + s;
         unsigned char f = 0;
-        if (a.eoff != nullptr && q >= 0 && q < a.N[2] && t8 < tiles_y8)
-          f = a.oflag == nullptr ? 1 : a.oflag[(blockIdx.x + (long long)gridDim.x * t8) * a.N[2] + q];
-        zf[t * NSUB + s] = f;
+        if (a.eoff != nullptr && q >= 0 && q < a.N[2] && tr < tiles_yr) {
+          if (ex.oflag_w != nullptr) f = ex.oflag_w[(blockIdx.x + (long long)gridDim.x * tr) * a.N[2] + q];
+          else if (a.oflag != nullptr) f = a.oflag[(blockIdx.x + (long long)gridDim.x * ((tr * RW) / 8)) * a.N[2] + q];
+          else f = 1;
+        }
+        zf[t * NW + s] = f;
       }
     }
   }
@@ -231,7 +236,7 @@ __global__ void __launch_bounds__(V2<R, RW, NS, EDR>::NT, MB)
     if (ering) {
       const int t = q - kfirst;
 #pragma unroll
-      for (int u = 0; u < NSUB; ++u) eo = eo || zf[t * NSUB + u] != 0 || (t > 0 && zf[(t - 1) * NSUB + u] != 0);
+      for (int u = 0; u < NW; ++u) eo = eo || zf[t * NW + u] != 0 || (t > 0 && zf[(t - 1) * NW + u] != 0);
     }
     const uint32_t bar = smem_u32(&bars[s]);
     mbar_expect(bar, (uint32_t)(G::PLANE_BYTES + (eo ? G::EO_BYTES : 0) + (edr ? G::ED_BYTES : 0)));
@@ -411,8 +416,10 @@ __global__ void __launch_bounds__(V2<R, RW, NS, EDR>::NT, MB)
       // diagonal term (½ of each of the two corners around an output; pinned
       // outputs take none); lane 31's column i0+32 and the last row's row
       // above arrive through the exchange after the barrier
-      const bool offd = zf[p0 * NSUB + jw / 8] != 0;
-      if (offd) {
+      const bool offd = zf[p0 * NW + w] != 0;
+      // corner terms with real averaging weights outside the PML
+      auto corners = [&](auto rc_tag) {
+        constexpr bool RCW = decltype(rc_tag)::value;
         const C wmx = xt[2 * (TX + 2) + lane + 1], wpx = xt[3 * (TX + 2) + lane + 1];
         const C wmz = zt[2 * KC2 + p0], wpz = zt[3 * KC2 + p0];
 #pragma unroll
@@ -438,14 +445,14 @@ __global__ void __launch_bounds__(V2<R, RW, NS, EDR>::NT, MB)
           const R exy = eps_off(s0, 0, jj, lane, k), eyz = eps_off(s0, 1, jj, lane, k),
                   ezx = eps_off(s0, 2, jj, lane, k);
           const R eyz1 = eps_off(s1, 1, jj, lane, k + 1), ezx1 = eps_off(s1, 2, jj, lane, k + 1);
-          const C ax = wsum<false>(wmx, exm, wpx, eo[r][0]);
-          const C ay = wsum<false>(wmy, eym, wpy, eo[r][1]);
-          const C az = wsum<false>(wmz, ezp[r], wpz, eo[r][2]);
+          const C ax = wsum<RCW>(wmx, exm, wpx, eo[r][0]);
+          const C ay = wsum<RCW>(wmy, eym, wpy, eo[r][1]);
+          const C az = wsum<RCW>(wmz, ezp[r], wpz, eo[r][2]);
           const C xcv = cadd(cscale(ay, exy), cscale(az, ezx));
           const C ycv = cadd(cscale(ax, exy), cscale(az, eyz));
           const C zc0 = zvalid ? zcn[r] : cadd(cscale(ax, ezx), cscale(ay, eyz));
-          const C ax1 = wsum<false>(wmx, exm1, wpx, enx);
-          const C ay1 = wsum<false>(wmy, eym1, wpy, eny);
+          const C ax1 = wsum<RCW>(wmx, exm1, wpx, enx);
+          const C ay1 = wsum<RCW>(wmy, eym1, wpy, eny);
           const C zc1 = cadd(cscale(ax1, ezx1), cscale(ay1, eyz1));
           zcn[r] = zc1;
           C xn = shfl_down1(xcv);
@@ -460,12 +467,16 @@ __global__ void __launch_bounds__(V2<R, RW, NS, EDR>::NT, MB)
             xc_.yc[w][lane] = ycv;
           }
         }
+      };
+      if (offd) {
+        if (rc) corners(std::true_type{});
+        else corners(std::false_type{});
       } else {
         // a warp without off-diagonal terms leaves zeros for its neighbours
         xc_.yc[w][lane] = czero<C>();
       }
       zvalid = offd;
-      if (w == 2 && lane < TYT && zf[p0 * NSUB + lane / 8]) {
+      if (w == 2 && lane < TYT && zf[p0 * NW + lane / RW]) {
         // x-directed corner terms at column i0+32, tile row `lane`
         const int jj = lane;
         const bool pj = WALL && j0 + jj == 0;
@@ -477,7 +488,7 @@ __global__ void __launch_bounds__(V2<R, RW, NS, EDR>::NT, MB)
         const C ay = wsum<false>(wmy, eym, wpy, ey0);
         const C az = wsum<false>(zt[2 * KC2 + p0], ezm, zt[3 * KC2 + p0], ez0);
         xc_.xce[jj] = cadd(cscale(ay, eps_off(s0, 0, jj, TX, k)), cscale(az, eps_off(s0, 2, jj, TX, k)));
-      } else if (w == 3 && zf[p0 * NSUB + NSUB - 1]) {
+      } else if (w == 3 && zf[p0 * NW + NW - 1]) {
         // y-directed corner terms at row j0+TYT
         const int jj = TYT;
         const C exm = zif(z0, ev2<R, RW, NS>(sm, s0, 0, jj, lane - 1));
@@ -708,6 +719,7 @@ static int launch_v2_t(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R
   dmap = map;
   ex.eoff_tma = emap_v2<R, RW, NS>(h, &emap) ? 1 : 0;
   ex.ediag_tma = dmap_v2<R, RW, NS, EDR>(h, &dmap) ? 1 : 0;
+  ex.oflag_w = h->has_off ? h->oflag_rows[RW - 1] : nullptr;
   const OpArgs<R> a = op_args<R>(h);
   const cudaError_t e = launch_k(h, k_apply_v2<R, EPI, RW, NS, MB, EDR>, grid, dim3(G::NT, 1, 1), (size_t)G::SMEM, map, emap,
                                  dmap, a, ex, x, y, aux0, h->red, fin, sc, h->dev_err);
