@@ -432,7 +432,7 @@ struct Solve {
     bb = tmp.dot1.x;
     *st = fdfd_stats{};
     if (!std::isfinite(bb)) {
-      st->status = FDFD_ERR_NONFINITE;
+      st->status = status = FDFD_ERR_NONFINITE;
       done = true;
       return set_error(h, FDFD_ERR_NONFINITE, "the right-hand side holds a NaN or Inf");
     }
@@ -448,7 +448,7 @@ struct Solve {
     TRY(true_residual(h, b, tr, &rr));
     st->matvecs = 1;
     if (!std::isfinite(rr)) {
-      st->status = FDFD_ERR_NONFINITE;
+      st->status = status = FDFD_ERR_NONFINITE;
       done = true;
       return set_error(h, FDFD_ERR_NONFINITE, "the initial residual holds a NaN or Inf (check x0)");
     }

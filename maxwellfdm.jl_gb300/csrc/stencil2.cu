@@ -323,8 +323,8 @@ __global__ void __launch_bounds__(V2<R, RW, NS, EDR>::NT, MB)
       const int p0 = k - kfirst;
       X &xc_ = xch[k & 1];
       const bool z0 = WALL && k == 0;
-      // diagonal ε of plane k+1 and the epilogue operand at plane k: their
-      // latency overlaps this plane's curls
+      // diagonal ε (when it does not come through the ring) and the epilogue
+      // operand at plane k: their latency overlaps this plane's curls
       R epk[RW][3];
       C aux[RW][3];
 #pragma unroll
