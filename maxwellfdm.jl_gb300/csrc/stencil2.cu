@@ -179,6 +179,21 @@ __global__ void __launch_bounds__(V2<R, RW, NS, EDR>::NT, MB)
     if (ering) asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&emap)) : "memory");
     if (edr) asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&dmap)) : "memory");
   }
+  pdl_wait();
+  if (sc != nullptr && sc->done) return;  // every thread, before any copy is issued
+  // the first planes' E tiles go out now, so their latency overlaps the
+  // coefficient tables below; each slot's single arrival (and its ε tiles,
+  // which need the off-diagonal flags) follows once the tables are in place
+  if (tid == 0) {
+    for (int p = 0; p < NS; ++p) {
+      const int q = kfirst + p;
+      if (q <= k1) {
+        const uint32_t bar = smem_u32(&bars[p]);
+        mbar_expect_only(bar, (uint32_t)G::PLANE_BYTES);
+        tma_copy3d(smem_u32(sm + p * G::SLOT), &tmap, cx, cy, q, bar);
+      }
+    }
+  }
   if (tid >= 160 && tid < 160 + TX + 2) {  // x coefficients, columns −1 … TX
     const int t = tid - 160;
     const int c = cidx(a, 0, i0 + t - 1);
@@ -225,13 +240,12 @@ __global__ void __launch_bounds__(V2<R, RW, NS, EDR>::NT, MB)
   const bool rx = i0 - 1 >= a.rlo[0] && i0 + TX <= a.rhi[0];
   const bool ry = j0 + jw - 1 >= a.rlo[1] && j0 + jw + RW <= a.rhi[1];
 
-  pdl_wait();
-  if (sc != nullptr && sc->done) return;
   __syncthreads();
   // the copies of plane q into ring slot s: the E tile, and the off-diagonal
   // ε of the tile when plane q or q−1 carries off-diagonal terms (the
-  // z-directed corners of q serve both)
-  auto issue = [&](int q, int s) {
+  // z-directed corners of q serve both); with_e = false completes a slot
+  // whose E tile is already on its way
+  auto issue = [&](int q, int s, bool with_e) {
     bool eo = false;
     if (ering) {
       const int t = q - kfirst;
@@ -239,15 +253,17 @@ __global__ void __launch_bounds__(V2<R, RW, NS, EDR>::NT, MB)
       for (int u = 0; u < NW; ++u) eo = eo || zf[t * NW + u] != 0 || (t > 0 && zf[(t - 1) * NW + u] != 0);
     }
     const uint32_t bar = smem_u32(&bars[s]);
-    mbar_expect(bar, (uint32_t)(G::PLANE_BYTES + (eo ? G::EO_BYTES : 0) + (edr ? G::ED_BYTES : 0)));
-    tma_copy3d(smem_u32(sm + s * G::SLOT), &tmap, cx, cy, q, bar);
+    const uint32_t bytes = (with_e ? G::PLANE_BYTES : 0) + (eo ? G::EO_BYTES : 0) + (edr ? G::ED_BYTES : 0);
+    if (bytes) mbar_expect_only(bar, bytes);
+    if (with_e) tma_copy3d(smem_u32(sm + s * G::SLOT), &tmap, cx, cy, q, bar);
     if (eo) tma_copy4d(smem_u32(sm + G::EO_OFF + s * G::EO_SLOT), &emap, i0, j0, q, 0, bar);
     if (edr) tma_copy4d(smem_u32(sm + G::ED_OFF + s * G::ED_SLOT), &dmap, i0, j0, q, 0, bar);
+    mbar_arrive(bar);
   };
   if (tid == 0) {
     for (int p = 0; p < NS; ++p) {
       const int q = kfirst + p;
-      if (q <= k1) issue(q, p);
+      if (q <= k1) issue(q, p, false);
     }
   }
   // off-diagonal pair p at tile corner (ii, jj) of the plane in slot s
@@ -510,7 +526,7 @@ __global__ void __launch_bounds__(V2<R, RW, NS, EDR>::NT, MB)
         const int q = k - 1 + NS;  // the plane that takes plane k−1's slot
         if (q <= k1) {
           asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-          issue(q, sm1);
+          issue(q, sm1, true);
         }
       }
       // ---- outputs y(k)

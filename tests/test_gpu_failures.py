@@ -91,3 +91,30 @@ def test_bounded_wait_reports_timeout(pkg, oracle, monkeypatch):
     ref = S.A @ x
     assert np.linalg.norm(y - ref) / np.linalg.norm(ref) < 1e-5
     B.close()
+
+
+def test_multi_solve_reports_a_nonfinite_entry(pkg, oracle):
+    """fdfd_solve_multi with one NaN right-hand side among good ones: the call
+    reports FDFD_ERR_NONFINITE, the other entries are still solved."""
+    import torch
+    S = _system(oracle, (16, 14, 12))
+    A = _operator(pkg, S)
+    dev = torch.device("cuda", 0)
+    b = S.b()
+    bad = b.copy()
+    bad[3] = np.nan
+    bufs = []
+    for v in (b, bad, 2.0 * b):
+        bd = torch.from_numpy(v.view(np.float64).reshape(-1, 2)).to(dev)
+        bufs.append((bd, torch.zeros_like(bd)))
+    with pytest.raises(pkg.FDFDError) as ei:
+        pkg.solve_multi([(A, bd.data_ptr(), xd.data_ptr()) for bd, xd in bufs], tol=1e-8, precision="mixed")
+    assert ei.value.code == FDFD_ERR_NONFINITE
+    st = ei.value.stats
+    assert st[1]["status"] == FDFD_ERR_NONFINITE
+    for q in (0, 2):
+        assert st[q]["status"] == 0 and st[q]["relres"] <= 1e-8
+        x = bufs[q][1].cpu().numpy().view(np.complex128).reshape(-1)
+        bq = b if q == 0 else 2.0 * b
+        assert np.linalg.norm(bq - S.A @ x) / np.linalg.norm(bq) < 1.02e-8
+    A.close()
