@@ -124,8 +124,18 @@ __host__ __device__ __forceinline__ uint32_t shadow_hash(uint32_t x) {
 template <typename R>
 __device__ __forceinline__ typename CT<R>::C shadow(long long dof) {
   const uint32_t hsh = shadow_hash((uint32_t)dof);
-  const int re = (int)(int16_t)(hsh & 0xffffu), im = (int)(int16_t)(hsh >> 16);
-  return mk(R(re) * R(1.0 / 32768.0), R(im) * R(1.0 / 32768.0));
+  if constexpr (sizeof(R) == 4) {
+    // the same values without integer→float conversions: a half h, read as
+    // signed, is (h ^ 0x8000) − 32768; the float with bits 0x4B000000 | v is
+    // 2²³ + v exactly, and (2²³ + v)·2⁻¹⁵ − (2⁸ + 1) = (v − 32768)/32768
+    // is exact in one fused multiply-add per lane
+    const float2 b = make_float2(__uint_as_float(0x4B000000u | ((hsh & 0xffffu) ^ 0x8000u)),
+                                 __uint_as_float(0x4B000000u | ((hsh >> 16) ^ 0x8000u)));
+    return __ffma2_rn(b, make_float2(1.0f / 32768.0f, 1.0f / 32768.0f), make_float2(-257.0f, -257.0f));
+  } else {
+    const int re = (int)(int16_t)(hsh & 0xffffu), im = (int)(int16_t)(hsh >> 16);
+    return mk(R(re) * R(1.0 / 32768.0), R(im) * R(1.0 / 32768.0));
+  }
 }
 
 template <typename R>

@@ -22,7 +22,8 @@
 //     i0−1 (warp 1), and on planes carrying off-diagonal ε the corner terms
 //     of column i0+32 (warp 2) and row j0+TYT (warp 3);
 //   * one __syncthreads per plane (the exchange); the ring slot of plane
-//     k−1 is refilled right after it;
+//     k−1 is refilled right after it, by the last warp (warp 0 already
+//     carries a halo job);
 //   * pinned DOFs (tangential E on the low PEC walls, kept in the vector
 //     but outside Cₑ) are zeroed as they are loaded, so no fix-up pass
 //     touches the ring; the diagonal ε term uses their true values;
@@ -88,7 +89,8 @@ struct V2 {
   static constexpr int YT_OFF = XT_OFF + 4 * XT_N * (int)sizeof(C);
   static constexpr int ZT_OFF = YT_OFF + 4 * (TYT + 2) * (int)sizeof(C);
   static constexpr int ZF_OFF = ZT_OFF + 4 * KC2 * (int)sizeof(C);
-  static constexpr int BAR_OFF = (ZF_OFF + KC2 * NW + 15) / 16 * 16;
+  static constexpr int ZA_OFF = ZF_OFF + KC2 * NW;  // per plane: any strip flagged
+  static constexpr int BAR_OFF = (ZA_OFF + KC2 + 15) / 16 * 16;
   static constexpr int SMEM = BAR_OFF + NS * 8;
   static_assert(SLOT % 128 == 0 && EXCH_OFF % 128 == 0, "TMA destination alignment");
   static_assert(SMEM <= 227 * 1024, "shared memory per CTA");
@@ -115,11 +117,64 @@ __device__ __forceinline__ C shfl_down1(C v) {
   return mk(__shfl_down_sync(0xffffffffu, v.x, 1), __shfl_down_sync(0xffffffffu, v.y, 1));
 }
 
-// a·u + b·v for coefficients a, b that are real when RC
-template <bool RC, typename C>
-__device__ __forceinline__ C wsum(C a, C u, C b, C v) {
+
+// Complex64 arithmetic of the curls and the diagonal term on the paired FP32
+// instructions of sm_100 and later (__fadd2_rn, __fmul2_rn, __ffma2_rn:
+// both lanes rounded to nearest, as the scalar forms are), half the
+// instructions of the scalar forms; complex128 keeps the scalar forms.
+__device__ __forceinline__ float2 f2(float s) { return make_float2(s, s); }
+__device__ __forceinline__ float2 psub(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ double2 psub(double2 a, double2 b) { return csub(a, b); }
+// a·s + b for real s
+__device__ __forceinline__ float2 pfma(float2 a, float s, float2 b) { return __ffma2_rn(a, f2(s), b); }
+__device__ __forceinline__ double2 pfma(double2 a, double s, double2 b) { return cadd(cscale(a, s), b); }
+// a·u − b·v for coefficients a, b that are real when RC
+template <bool RC>
+__device__ __forceinline__ float2 pdiff(float2 a, float2 u, float2 b, float2 v) {
+  if constexpr (RC) {
+    return __ffma2_rn(f2(a.x), u, __fmul2_rn(f2(-b.x), v));
+  } else {
+    float2 t = __fmul2_rn(make_float2(b.y, -b.y), make_float2(v.y, v.x));  // −b·v
+    t = __ffma2_rn(f2(-b.x), v, t);
+    t = __ffma2_rn(make_float2(-a.y, a.y), make_float2(u.y, u.x), t);     // + a·u
+    return __ffma2_rn(f2(a.x), u, t);
+  }
+}
+template <bool RC>
+__device__ __forceinline__ double2 pdiff(double2 a, double2 u, double2 b, double2 v) {
+  return csub(mulc<RC>(a, u), mulc<RC>(b, v));
+}
+// conj(a0)·b0 + conj(a1)·b1 + conj(a2)·b2
+__device__ __forceinline__ float2 pdot3(float2 a0, float2 b0, float2 a1, float2 b1, float2 a2, float2 b2) {
+  float2 t = __fmul2_rn(f2(a0.x), b0);
+  t = __ffma2_rn(make_float2(a0.y, -a0.y), make_float2(b0.y, b0.x), t);
+  t = __ffma2_rn(f2(a1.x), b1, t);
+  t = __ffma2_rn(make_float2(a1.y, -a1.y), make_float2(b1.y, b1.x), t);
+  t = __ffma2_rn(f2(a2.x), b2, t);
+  return __ffma2_rn(make_float2(a2.y, -a2.y), make_float2(b2.y, b2.x), t);
+}
+__device__ __forceinline__ double2 pdot3(double2 a0, double2 b0, double2 a1, double2 b1, double2 a2, double2 b2) {
+  return cadd(cadd(cdotc(a0, b0), cdotc(a1, b1)), cdotc(a2, b2));
+}
+// a·u + b·v for coefficients a, b that are real when RC (corner averaging)
+template <bool RC>
+__device__ __forceinline__ float2 wsum(float2 a, float2 u, float2 b, float2 v) {
   return cadd(mulc<RC>(a, u), mulc<RC>(b, v));
 }
+template <bool RC>
+__device__ __forceinline__ double2 wsum(double2 a, double2 u, double2 b, double2 v) {
+  return cadd(mulc<RC>(a, u), mulc<RC>(b, v));
+}
+// u·s + v·t for real s, t
+__device__ __forceinline__ float2 pmix(float2 u, float s, float2 v, float t) {
+  return __ffma2_rn(u, f2(s), __fmul2_rn(v, f2(t)));
+}
+__device__ __forceinline__ double2 pmix(double2 u, double s, double2 v, double t) {
+  return cadd(cscale(u, s), cscale(v, t));
+}
+// (u + v)·s for real s
+__device__ __forceinline__ float2 psums(float2 u, float2 v, float s) { return __fmul2_rn(__fadd2_rn(u, v), f2(s)); }
+__device__ __forceinline__ double2 psums(double2 u, double2 v, double s) { return cscale(cadd(u, v), s); }
 
 template <typename R>
 struct Accs2 {
@@ -151,6 +206,7 @@ __global__ void __launch_bounds__(V2<R, RW, NS, EDR>::NT, MB)
   C *yt = reinterpret_cast<C *>(sm + G::YT_OFF);
   C *zt = reinterpret_cast<C *>(sm + G::ZT_OFF);
   unsigned char *zf = sm + G::ZF_OFF;
+  unsigned char *za = sm + G::ZA_OFF;
   uint64_t *bars = reinterpret_cast<uint64_t *>(sm + G::BAR_OFF);
   pdl_trigger();
 
@@ -221,6 +277,7 @@ __global__ void __launch_bounds__(V2<R, RW, NS, EDR>::NT, MB)
       // one flag per warp strip (RW rows): its outputs at plane q read a
       // non-zero off-diagonal ε (the 32×8 tile flags stand in when the
       // strip flags are absent)
+      unsigned char any = 0;
 #pragma unroll
       for (int s = 0; s < NW; ++s) {
         const int tr = j0 / RW + s;
@@ -231,7 +288,9 @@ __global__ void __launch_bounds__(V2<R, RW, NS, EDR>::NT, MB)
           else f = 1;
         }
         zf[t * NW + s] = f;
+        any |= f;
       }
+      za[t] = any;
     }
   }
   const int cxi = cidx(a, 0, gi);
@@ -249,8 +308,7 @@ __global__ void __launch_bounds__(V2<R, RW, NS, EDR>::NT, MB)
     bool eo = false;
     if (ering) {
       const int t = q - kfirst;
-#pragma unroll
-      for (int u = 0; u < NW; ++u) eo = eo || zf[t * NW + u] != 0 || (t > 0 && zf[(t - 1) * NW + u] != 0);
+      eo = za[t] != 0 || (t > 0 && za[t - 1] != 0);
     }
     const uint32_t bar = smem_u32(&bars[s]);
     const uint32_t bytes = (with_e ? G::PLANE_BYTES : 0) + (eo ? G::EO_BYTES : 0) + (edr ? G::ED_BYTES : 0);
@@ -391,13 +449,13 @@ __global__ void __launch_bounds__(V2<R, RW, NS, EDR>::NT, MB)
         }
         const C eny = zif(pin_i, en[r][1]), enx = zif(pin_j[r], en[r][0]);
         if (rc) {
-          hx[r] = csub(mulc<true>(cmy, csub(ezj, eo[r][2])), mulc<true>(cmz, csub(eny, eo[r][1])));
-          hy[r] = csub(mulc<true>(cmz, csub(enx, eo[r][0])), mulc<true>(cmx, csub(ezi, eo[r][2])));
-          hz[r] = csub(mulc<true>(cmx, csub(eyi, eo[r][1])), mulc<true>(cmy, csub(exj, eo[r][0])));
+          hx[r] = pdiff<true>(cmy, psub(ezj, eo[r][2]), cmz, psub(eny, eo[r][1]));
+          hy[r] = pdiff<true>(cmz, psub(enx, eo[r][0]), cmx, psub(ezi, eo[r][2]));
+          hz[r] = pdiff<true>(cmx, psub(eyi, eo[r][1]), cmy, psub(exj, eo[r][0]));
         } else {
-          hx[r] = csub(cmul(cmy, csub(ezj, eo[r][2])), cmul(cmz, csub(eny, eo[r][1])));
-          hy[r] = csub(cmul(cmz, csub(enx, eo[r][0])), cmul(cmx, csub(ezi, eo[r][2])));
-          hz[r] = csub(cmul(cmx, csub(eyi, eo[r][1])), cmul(cmy, csub(exj, eo[r][0])));
+          hx[r] = pdiff<false>(cmy, psub(ezj, eo[r][2]), cmz, psub(eny, eo[r][1]));
+          hy[r] = pdiff<false>(cmz, psub(enx, eo[r][0]), cmx, psub(ezi, eo[r][2]));
+          hz[r] = pdiff<false>(cmx, psub(eyi, eo[r][1]), cmy, psub(exj, eo[r][0]));
         }
       }
       // last row's H_x, H_z for the warp above
@@ -522,7 +580,8 @@ __global__ void __launch_bounds__(V2<R, RW, NS, EDR>::NT, MB)
         kstop = k;
         break;
       }
-      if (tid == 0) {
+      // the refill goes out from the last warp, which has no halo job
+      if (tid == G::NT - 32) {
         const int q = k - 1 + NS;  // the plane that takes plane k−1's slot
         if (q <= k1) {
           asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -543,13 +602,13 @@ __global__ void __launch_bounds__(V2<R, RW, NS, EDR>::NT, MB)
         }
         C yx, yy, yz;
         if (rc) {
-          yx = csub(mulc<true>(cey, csub(hz[r], hzjm)), mulc<true>(cez, csub(hy[r], hyp[r])));
-          yy = csub(mulc<true>(cez, csub(hx[r], hxp[r])), mulc<true>(cex, csub(hz[r], hzim)));
-          yz = csub(mulc<true>(cex, csub(hy[r], hyim)), mulc<true>(cey, csub(hx[r], hxjm)));
+          yx = pdiff<true>(cey, psub(hz[r], hzjm), cez, psub(hy[r], hyp[r]));
+          yy = pdiff<true>(cez, psub(hx[r], hxp[r]), cex, psub(hz[r], hzim));
+          yz = pdiff<true>(cex, psub(hy[r], hyim), cey, psub(hx[r], hxjm));
         } else {
-          yx = csub(cmul(cey, csub(hz[r], hzjm)), cmul(cez, csub(hy[r], hyp[r])));
-          yy = csub(cmul(cez, csub(hx[r], hxp[r])), cmul(cex, csub(hz[r], hzim)));
-          yz = csub(cmul(cex, csub(hy[r], hyim)), cmul(cey, csub(hx[r], hxjm)));
+          yx = pdiff<false>(cey, psub(hz[r], hzjm), cez, psub(hy[r], hyp[r]));
+          yy = pdiff<false>(cez, psub(hx[r], hxp[r]), cex, psub(hz[r], hzim));
+          yz = pdiff<false>(cex, psub(hy[r], hyim), cey, psub(hx[r], hxjm));
         }
         const bool px = pin_j[r] || z0, py = pin_i || z0, pz = pin_i || pin_j[r];
         // Pε E at the cell: the diagonal with the true E (the ring slot of
@@ -571,10 +630,10 @@ __global__ void __launch_bounds__(V2<R, RW, NS, EDR>::NT, MB)
           if (py) t1 = ev2<R, RW, NS>(sm, s0, 1, jj, lane);
           if (pz) t2 = ev2<R, RW, NS>(sm, s0, 2, jj, lane);
         }
-        C d0 = cadd(cscale(t0, e0), od[r][0]), d1 = cadd(cscale(t1, e1), od[r][1]), d2 = cadd(cscale(t2, e2), od[r][2]);
+        C d0 = pfma(t0, e0, od[r][0]), d1 = pfma(t1, e1, od[r][1]), d2 = pfma(t2, e2, od[r][2]);
         if (offd) {
-          if (lane == TX - 1 && !px) d0 = cadd(d0, cscale(xc_.xce[jj], R(0.5)));
-          if (r == RW - 1 && !py) d1 = cadd(d1, cscale(xc_.yc[w + 1][lane], R(0.5)));
+          if (lane == TX - 1 && !px) d0 = pfma(xc_.xce[jj], R(0.5), d0);
+          if (r == RW - 1 && !py) d1 = pfma(xc_.yc[w + 1][lane], R(0.5), d1);
         }
         if (WALL) {
           if (px) yx = czero<C>();
@@ -582,9 +641,9 @@ __global__ void __launch_bounds__(V2<R, RW, NS, EDR>::NT, MB)
           if (pz) yz = czero<C>();
         }
         if (a.w2.y == R(0)) {
-          yx = csub(yx, cscale(d0, a.w2.x));
-          yy = csub(yy, cscale(d1, a.w2.x));
-          yz = csub(yz, cscale(d2, a.w2.x));
+          yx = pfma(d0, -a.w2.x, yx);
+          yy = pfma(d1, -a.w2.x, yy);
+          yz = pfma(d2, -a.w2.x, yz);
         } else {
           yx = csub(yx, cmul(a.w2, d0));
           yy = csub(yy, cmul(a.w2, d1));
@@ -609,10 +668,9 @@ __global__ void __launch_bounds__(V2<R, RW, NS, EDR>::NT, MB)
             acc.i0.add(q0.y + q1.y + q2.y);
             acc.r1.add(yx.x * yx.x + yx.y * yx.y + yy.x * yy.x + yy.y * yy.y + yz.x * yz.x + yz.y * yz.y);
           } else if (EPI == EPI_DOT_SHD) {
-            const C q0 = cdotc(shadow<R>(3ll * ce), yx), q1 = cdotc(shadow<R>(3ll * ce + 1), yy),
-                    q2 = cdotc(shadow<R>(3ll * ce + 2), yz);
-            acc.r0.add(q0.x + q1.x + q2.x);
-            acc.i0.add(q0.y + q1.y + q2.y);
+            const C q = pdot3(shadow<R>(3ll * ce), yx, shadow<R>(3ll * ce + 1), yy, shadow<R>(3ll * ce + 2), yz);
+            acc.r0.add(q.x);
+            acc.i0.add(q.y);
           }
           C *yo = y + 3 * ce;
           yo[0] = yx;
