@@ -33,6 +33,13 @@ sys.path.insert(0, ROOT)
 METRIC = "time to 1e-6 rel. residual, mixed vs FP64 on same GB300; matvec HBM GB/s"
 WORKLOAD = "96^3 dielectric-sphere scatterer: 40 spheres r~U[3,8] eps=12.25, 10-cell PML, lambda=16, x-pol sheet z=15"
 METHOD, ELL = "bicgstabl", 4   # BiCGStab(4) in both precisions
+# The mixed solve stops at a 5e-7 true residual with reliable updates every
+# 100-fold residual drop: at a 1e-6 stop its field error against an accurate
+# FP64 solution was 0.7-1.9e-5 (error/residual ratios of 11-31 on this
+# system, depending on where in a residual drop the stop falls), at 5e-7 it
+# stays near 5e-6.  The timed mixed solve therefore reaches a stricter
+# residual than the FP64 one it is compared with.
+MIXED_TOL, MIXED_DELTA = 5e-7, 0.01
 
 
 def _dist():
@@ -276,7 +283,8 @@ def run_ours(args):
     x_dev = torch.zeros_like(b_dev)
     tol = 1e-6
     for _ in range(args.warmup):
-        A.solve_dev(b_dev.data_ptr(), x_dev.data_ptr(), tol=tol, precision="mixed", method=METHOD, ell=ELL)
+        A.solve_dev(b_dev.data_ptr(), x_dev.data_ptr(), tol=MIXED_TOL, precision="mixed", method=METHOD, ell=ELL,
+                    delta=MIXED_DELTA)
     torch.cuda.synchronize(dev)
     _barrier(ws)
     clk = ClockSampler(local)
@@ -287,7 +295,8 @@ def run_ours(args):
     torch.cuda.synchronize(dev)
     for _ in range(args.steps):
         ev0.record(stream)
-        st = A.solve_dev(b_dev.data_ptr(), x_dev.data_ptr(), tol=tol, precision="mixed", method=METHOD, ell=ELL)
+        st = A.solve_dev(b_dev.data_ptr(), x_dev.data_ptr(), tol=MIXED_TOL, precision="mixed", method=METHOD, ell=ELL,
+                         delta=MIXED_DELTA)
         ev1.record(stream)
         ev1.synchronize()
         times.append(ev0.elapsed_time(ev1) / 1e3)
@@ -367,8 +376,8 @@ def run_ours(args):
     e2e_t = []
     for _ in range(max(1, args.steps)):
         t0 = time.perf_counter()
-        xs, _st = A.solve(bh.numpy().view(np.complex128).reshape(-1), tol=tol, precision="mixed", method=METHOD,
-                         ell=ELL)
+        xs, _st = A.solve(bh.numpy().view(np.complex128).reshape(-1), tol=MIXED_TOL, precision="mixed", method=METHOD,
+                          ell=ELL, delta=MIXED_DELTA)
         e2e_t.append(time.perf_counter() - t0)
     e2e = max_over_ranks(statistics.mean(e2e_t), ws, dev)
 
@@ -390,7 +399,7 @@ def run_ours(args):
             "vs_baseline": None, "dtype": "c64 (double-float FP32 reductions, FP64 residual replacement)",
             "data": "synthetic (seeded spheres, seed 1000+rank)",
             "config": {"workload": WORKLOAD, "cells": A.ncell, "unknowns": n, "solver": "BiCGStab(4)",
-                       "tol": tol, "l2": "solve working set > L2 (12 c64 + 3 c128 vectors = 0.38 GB); L2 "
+                       "tol": tol, "mixed_stop": MIXED_TOL, "mixed_delta": MIXED_DELTA, "l2": "solve working set > L2 (12 c64 + 3 c128 vectors = 0.38 GB); L2 "
                                          "flushed by a 256 MiB read before each roofline launch",
                        "parallelism": "replicas" if ws > 1 else "1 GPU"},
             "fp64_time_s": t_fp64, "mixed_speedup_vs_fp64": t_fp64 / t_mixed,
