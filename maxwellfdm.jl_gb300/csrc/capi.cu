@@ -519,6 +519,8 @@ void fdfd_destroy(fdfd_handle *h) {
     cudaFree(h->oflag_rows[0]);
     cudaFree(h->oflag_rows[1]);
     cudaFree(h->smask);
+    cudaFree(h->work[0]);
+    cudaFree(h->work[1]);
   }
   cudaFree(h->vx64);
   cudaFree(h->vy64);
@@ -759,6 +761,10 @@ static fdfd_handle *make_worker(fdfd_handle *p, int *rc) {
   w->pdl = p->pdl;
   w->kc[0] = p->kc[0];
   w->kc[1] = p->kc[1];
+  for (int q = 0; q < 2; ++q) {
+    w->work[q] = p->work[q];
+    w->nwork[q] = p->nwork[q];
+  }
   w->kc_force = p->kc_force;
   w->wait_limit = p->wait_limit;
   w->op_variant = p->op_variant;

@@ -157,6 +157,11 @@ struct fdfd_handle {
   bool tma_disabled = false;          // FDFD_DISABLE_TMA=1: plain-load operator kernel only
   bool pdl = false;                   // programmatic dependent launch (FDFD_PDL=1 enables)
   int kc[2] = {0, 0};                 // tuned z-chunk length: [complex128, complex64]
+  // second TMA kernel: a balanced schedule per precision (same order) of
+  // (x tile, y tile, k0, k1) per thread block, heaviest first, when the
+  // tuner found it faster than uniform chunks (nwork 0: uniform)
+  int4 *work[2] = {nullptr, nullptr};
+  int nwork[2] = {0, 0};
   int kc_force = 0;                   // FDFD_KCHUNK: fixed z-chunk length (no tuning)
   // SM clocks a pipeline wait of the TMA operator kernel may take before it
   // gives up (≈1 s); FDFD_WAIT_LIMIT_CLOCKS lowers it, so that a test can

@@ -20,6 +20,7 @@ struct Extra {
   int ediag_tma;      // second TMA kernel: ε diagonal staged through the ring
   const uint8_t *oflag_w;  // second TMA kernel: off-diagonal flags per x tile, warp strip and plane
   long long wait_limit;  // TMA kernel: SM clocks a pipeline wait may take before it gives up
+  const int4 *work;      // second TMA kernel: (x tile, y tile, k0, k1) per block, or null (uniform chunks)
 };
 
 template <typename R>

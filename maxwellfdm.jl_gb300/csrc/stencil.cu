@@ -28,8 +28,11 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <utility>
+#include <vector>
 
 #include "krylov_fin.cuh"
 #include "operator_common.cuh"
@@ -800,7 +803,7 @@ static int blocks_for(const fdfd_handle *h, int kc) {
 
 int apply_blocks(const fdfd_handle *h) {
   const int a = blocks_for(h, kchunk_for(h, true)), b = blocks_for(h, kchunk_for(h, false));
-  return a > b ? a : b;
+  return std::max(std::max(a, b), std::max(h->nwork[0], h->nwork[1]));
 }
 
 template <typename R>
@@ -812,6 +815,7 @@ Extra<R> make_extra(const fdfd_handle *h) {
   ex.ediag_tma = 0;
   ex.oflag_w = nullptr;
   ex.wait_limit = h->wait_limit;
+  ex.work = nullptr;
   const C *coef;
   if constexpr (sizeof(R) == 8) coef = reinterpret_cast<const C *>(h->coef64);
   else coef = reinterpret_cast<const C *>(h->coef32);
@@ -942,16 +946,115 @@ static int launch_t(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R>::
   return cuda_check(h, e, "k_apply launch");
 }
 
+// Reads a buffer larger than L2: evicts the operands of the next launch and,
+// unlike a memset, leaves no dirty lines whose write-back would be charged
+// to it.  The sink is written only if the running xor meets a value the
+// buffer's contents never produce, which keeps the loads.
+__global__ void k_read_flush(const uint4 *__restrict__ p, size_t n, unsigned *sink) {
+  unsigned acc = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const uint4 v = p[i];
+    acc ^= v.x ^ v.y ^ v.z ^ v.w;
+  }
+  if (acc == 0x9e3779b9u) *sink = acc;
+}
+
+// Seeded values in [−1, 1) (the shadow vector's hash): the tuning input, so
+// that no candidate is timed on all-zero data.
+template <typename R>
+__global__ void k_fill_hash(typename CT<R>::C *x, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    x[i] = shadow<R>(i);
+}
+
+// Rows per warp strip of the second TMA kernel's layout (its tiles are 8
+// strips high).
+static int v2_rows_per_warp(const fdfd_handle *h, bool c64) {
+  if (!c64) return 1;
+  return (h->op_variant == 1 || h->op_variant == 3) ? 1 : 2;
+}
+
+// Balanced z-chunk schedule of the second TMA kernel for tiles of 8·rw rows.
+// In each (x tile, y tile) column a plane costs 1, or 1 + wcorner when a
+// warp strip of the tile-plane carries off-diagonal ε terms (every warp then
+// waits at the plane's barrier for that strip's corner work).  Each column
+// is cut at even cost thresholds into the fewest chunks of at most about
+// total/target cost (and at most KCMAX planes), and the chunks are listed
+// heaviest first, so that a launch of more than one wave starts them first.
+static void build_schedule(const fdfd_handle *h, const std::vector<uint8_t> &strip_flags, int rw, int target,
+                           double wcorner, std::vector<int4> &out) {
+  const int tyt = 8 * rw;
+  const int tx = (h->N[0] + TX - 1) / TX, ty = (h->N[1] + tyt - 1) / tyt, nz = h->N[2];
+  const int strips_y = (h->N[1] + rw - 1) / rw;
+  std::vector<double> cost((size_t)tx * ty * nz);
+  double total = 0;
+  for (int by = 0; by < ty; ++by)
+    for (int bx = 0; bx < tx; ++bx)
+      for (int q = 0; q < nz; ++q) {
+        bool f = false;
+        for (int st = 0; st < 8 && !strip_flags.empty() && !f; ++st) {
+          const int tr = by * 8 + st;
+          if (tr < strips_y) f = strip_flags[((size_t)bx + (size_t)tx * tr) * nz + q] != 0;
+        }
+        const double c = f ? 1.0 + wcorner : 1.0;
+        cost[((size_t)by * tx + bx) * nz + q] = c;
+        total += c;
+      }
+  // the per-column chunk counts round up: raise the goal until the total
+  // fits the target (a one-wave schedule must not spill into a second wave)
+  const int min_per_col = (nz + KCMAX - 1) / KCMAX;
+  std::vector<double> colcost((size_t)tx * ty, 0.0);
+  for (size_t col = 0; col < colcost.size(); ++col)
+    for (int q = 0; q < nz; ++q) colcost[col] += cost[col * nz + q];
+  double goal_all = total / std::max(1, target);
+  for (int it = 0; it < 200; ++it) {
+    long long count = 0;
+    for (const double cc : colcost) count += std::max((int)std::ceil(cc / goal_all - 1e-9), min_per_col);
+    if (count <= target) break;
+    goal_all *= 1.02;
+  }
+  std::vector<std::pair<double, int4>> chunks;
+  for (int by = 0; by < ty; ++by)
+    for (int bx = 0; bx < tx; ++bx) {
+      const double *c = &cost[((size_t)by * tx + bx) * nz];
+      double left_cost = colcost[(size_t)by * tx + bx];
+      int left = std::max((int)std::ceil(left_cost / goal_all - 1e-9), min_per_col);
+      int q = 0;
+      while (q < nz) {
+        const double goal = left_cost / std::max(left, 1);
+        const int k0 = q;
+        double acc = 0;
+        while (q < nz && q - k0 < KCMAX) {
+          acc += c[q++];
+          if (left > 1 && acc >= goal - 1e-9) break;
+        }
+        chunks.push_back({acc, make_int4(bx, by, k0, q)});
+        left_cost -= acc;
+        left = std::max(left - 1, 1);
+      }
+    }
+  std::stable_sort(chunks.begin(), chunks.end(),
+                   [](const std::pair<double, int4> &a, const std::pair<double, int4> &b) { return a.first > b.first; });
+  out.resize(chunks.size());
+  for (size_t i = 0; i < chunks.size(); ++i) out[i] = chunks[i].second;
+}
+
 // Autotuner for the z-chunk length (and, for complex64, the tile layout of
-// the second TMA kernel): times y = A x for each candidate with
-// CUDA events on the handle's stream — one warm-up, then three launches each
-// preceded by an L2 flush (a 192 MiB memset, larger than the 129 MB L2), so
-// the choice holds for inputs streamed from HBM — and keeps the fastest,
-// separately for complex64 and complex128.  Runs at fdfd_create (vacuum ε)
-// and again whenever new ε data switches the off-diagonal tensor on or off,
-// since the corner-term work changes the best chunk length.
+// the second TMA kernel, and for both its balanced schedules): times y = A x
+// for each candidate with CUDA events on the handle's stream — one warm-up,
+// then five launches each preceded by an L2 flush (a 192 MiB read, larger
+// than the 129 MB L2), the median counting — so the choice holds for inputs
+// streamed from HBM, and keeps the fastest, separately for complex64 and
+// complex128.  Runs at fdfd_create (vacuum ε) and again whenever new ε data
+// switches the off-diagonal tensor on or off, since the corner-term work
+// changes the best chunk length.
 int autotune_kchunk(fdfd_handle *h) {
   if (h->kc_force > 0) return FDFD_OK;
+  for (int p = 0; p < 2; ++p) {  // uniform chunks until a schedule wins again
+    cudaFree(h->work[p]);
+    h->work[p] = nullptr;
+    h->nwork[p] = 0;
+  }
   const size_t n = 3 * (size_t)h->ncell;
   const size_t flush_bytes = 192ull << 20;
   void *bx = nullptr, *by = nullptr, *fl = nullptr;
@@ -962,7 +1065,7 @@ int autotune_kchunk(fdfd_handle *h) {
     cudaFree(by);
     return set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(autotune buffers) failed");
   }
-  int rc = cuda_check(h, cudaMemsetAsync(bx, 0, n * sizeof(double2), h->stream), "memset");
+  int rc = cuda_check(h, cudaMemsetAsync(fl, 0, flush_bytes, h->stream), "memset");
   const int cand[] = {4, 6, 8, 12, 16, 24, 32, 48, 64};
   const bool verbose = std::getenv("FDFD_VERBOSE") != nullptr;
   // complex64 also picks the tile layout of the second TMA kernel (two rows
@@ -970,7 +1073,40 @@ int autotune_kchunk(fdfd_handle *h) {
   // unless FDFD_OPERATOR_V2 fixed it; complex128 has one layout
   const bool tune_layout = h->op_variant != 0 && std::getenv("FDFD_OPERATOR_V2") == nullptr;
   const int layouts_c64[] = {4, 1, 3};
+  int sms = 152;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->dev) != cudaSuccess) {
+    cudaGetLastError();
+    sms = 152;
+  }
   for (int prec = 0; prec < 2 && rc == FDFD_OK; ++prec) {
+    // median of five launches of the current configuration, each after an L2 flush
+    auto timed = [&](float *med) -> int {
+      auto launch = [&]() {
+        return prec == 1 ? launch_apply_fin<float>(h, (const float2 *)bx, (float2 *)by, EPI_STORE, nullptr,
+                                                   FIN_NONE, nullptr, false)
+                         : launch_apply_fin<double>(h, (const double2 *)bx, (double2 *)by, EPI_STORE, nullptr,
+                                                    FIN_NONE, nullptr, false);
+      };
+      int r2 = launch();
+      float ts[5];
+      for (int r = 0; r < 5 && r2 == FDFD_OK; ++r) {
+        k_read_flush<<<sms * 4, 512, 0, h->stream>>>((const uint4 *)fl, flush_bytes / sizeof(uint4) - 1,
+                                                      (unsigned *)fl + flush_bytes / sizeof(unsigned) - 1);
+        cudaEventRecord(h->ev0, h->stream);
+        r2 = launch();
+        cudaEventRecord(h->ev1, h->stream);
+        if (r2 || (r2 = cuda_check(h, cudaEventSynchronize(h->ev1), "autotune sync"))) break;
+        cudaEventElapsedTime(&ts[r], h->ev0, h->ev1);
+      }
+      if (r2 == FDFD_OK) {
+        std::sort(ts, ts + 5);
+        *med = ts[2];
+      }
+      return r2;
+    };
+    if (prec == 1) k_fill_hash<float><<<sms * 4, 256, 0, h->stream>>>((float2 *)bx, (long long)n);
+    else k_fill_hash<double><<<sms * 4, 256, 0, h->stream>>>((double2 *)bx, (long long)n);
+    if ((rc = cuda_check(h, cudaGetLastError(), "k_fill_hash"))) break;
     float best = 1e30f;
     int best_kc = 0, best_layout = h->op_variant;
     const int nlay = (prec == 1 && tune_layout) ? 3 : 1;
@@ -983,25 +1119,8 @@ int autotune_kchunk(fdfd_handle *h) {
         if (chunks == last_chunks) continue;
         last_chunks = chunks;
         h->kc[prec] = kc;
-        auto launch = [&]() {
-          return prec == 1 ? launch_apply_fin<float>(h, (const float2 *)bx, (float2 *)by, EPI_STORE, nullptr,
-                                                     FIN_NONE, nullptr, false)
-                           : launch_apply_fin<double>(h, (const double2 *)bx, (double2 *)by, EPI_STORE, nullptr,
-                                                      FIN_NONE, nullptr, false);
-        };
-        if ((rc = launch())) break;
-        float ts[5];
-        for (int r = 0; r < 5 && rc == FDFD_OK; ++r) {
-          cudaMemsetAsync(fl, r, flush_bytes, h->stream);
-          cudaEventRecord(h->ev0, h->stream);
-          rc = launch();
-          cudaEventRecord(h->ev1, h->stream);
-          if (rc || (rc = cuda_check(h, cudaEventSynchronize(h->ev1), "autotune sync"))) break;
-          cudaEventElapsedTime(&ts[r], h->ev0, h->ev1);
-        }
-        if (rc) break;
-        std::sort(ts, ts + 5);
-        const float med = ts[2];
+        float med = 0.f;
+        if ((rc = timed(&med))) break;
         if (verbose)
           fprintf(stderr, "fdfd autotune: %s layout %d kchunk %d: %.1f us\n", prec ? "c64" : "c128", h->op_variant,
                   kc, med * 1e3);
@@ -1016,6 +1135,87 @@ int autotune_kchunk(fdfd_handle *h) {
     }
     h->kc[prec] = best_kc;
     if (prec == 1 && tune_layout) h->op_variant = best_layout;
+    // the second TMA kernel can also run a balanced schedule: columns cut
+    // into chunks of equal estimated cost (planes with off-diagonal terms
+    // weigh more), for one to four waves of thread blocks
+    if (rc == FDFD_OK && best_kc > 0 && h->op_variant != 0) {
+      const int rw = v2_rows_per_warp(h, prec == 1);
+      std::vector<uint8_t> flags;
+      if (h->has_off && h->oflag_rows[rw - 1] != nullptr) {
+        flags.resize((size_t)((h->N[0] + TX - 1) / TX) * ((h->N[1] + rw - 1) / rw) * h->N[2]);
+        rc = cuda_check(h, cudaMemcpyAsync(flags.data(), h->oflag_rows[rw - 1], flags.size(), cudaMemcpyDeviceToHost,
+                                           h->stream), "copy strip flags");
+        if (rc == FDFD_OK) rc = cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
+      }
+      const int slots = sms * ((prec == 1 && h->op_variant == 1) ? 3 : 2);
+      // FDFD_SCHEDULE=w takes the w-wave schedule (weight 1) untimed, 0 none
+      const char *fs = std::getenv("FDFD_SCHEDULE");
+      const int forced = fs != nullptr ? std::atoi(fs) : -1;
+      std::vector<std::vector<int4>> scheds;
+      std::vector<double> weights;
+      for (int waves = 1; waves <= 4; ++waves)
+        for (const double wc : {0.5, 1.0}) {
+          if (!h->has_off && wc != 0.5) continue;  // no corner terms: one weight is enough
+          if (forced >= 0 && (waves != forced || wc != 1.0)) continue;
+          scheds.emplace_back();
+          build_schedule(h, flags, rw, waves * slots, h->has_off ? wc : 0.0, scheds.back());
+          weights.push_back(waves + 0.1 * wc);
+        }
+      // a schedule must hold every column's planes once, in chunks of 1 …
+      // KCMAX planes; one that does not is dropped (uniform chunks stay)
+      {
+        const int tyt = 8 * rw;
+        const int ncol = ((h->N[0] + TX - 1) / TX) * ((h->N[1] + tyt - 1) / tyt);
+        for (size_t c = 0; c < scheds.size(); ++c) {
+          long long planes = 0;
+          bool bad = scheds[c].empty();
+          for (const int4 &e : scheds[c]) {
+            bad = bad || e.w <= e.z || e.w - e.z > KCMAX || e.z < 0 || e.w > h->N[2];
+            planes += e.w - e.z;
+          }
+          if (bad || planes != (long long)ncol * h->N[2]) {
+            if (verbose) fprintf(stderr, "fdfd autotune: schedule %zu dropped (bad chunks)\n", c);
+            scheds.erase(scheds.begin() + c);
+            weights.erase(weights.begin() + c);
+            --c;
+          }
+        }
+      }
+      size_t cap = 0;
+      for (const auto &sc : scheds) cap = std::max(cap, sc.size());
+      int4 *dw = nullptr;
+      if (rc == FDFD_OK && dev_malloc(&dw, cap * sizeof(int4)) != cudaSuccess) {
+        cudaGetLastError();
+        rc = set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(schedule) failed");
+      }
+      int won = -1;
+      for (size_t c = 0; c < scheds.size() && rc == FDFD_OK; ++c) {
+        rc = cuda_check(h, cudaMemcpyAsync(dw, scheds[c].data(), scheds[c].size() * sizeof(int4),
+                                           cudaMemcpyHostToDevice, h->stream), "upload schedule");
+        if (rc) break;
+        h->work[prec] = dw;
+        h->nwork[prec] = (int)scheds[c].size();
+        float med = 0.f;
+        if ((rc = timed(&med))) break;
+        if (verbose)
+          fprintf(stderr, "fdfd autotune: %s layout %d schedule %.1f (%zu blocks): %.1f us\n", prec ? "c64" : "c128",
+                  h->op_variant, weights[c], scheds[c].size(), med * 1e3);
+        if (med < 0.97f * best || forced > 0) {
+          best = med;
+          won = (int)c;
+        }
+      }
+      if (rc == FDFD_OK && won >= 0) {
+        rc = cuda_check(h, cudaMemcpyAsync(dw, scheds[won].data(), scheds[won].size() * sizeof(int4),
+                                           cudaMemcpyHostToDevice, h->stream), "upload schedule");
+        h->work[prec] = dw;
+        h->nwork[prec] = (int)scheds[won].size();
+      } else {
+        h->work[prec] = nullptr;
+        h->nwork[prec] = 0;
+        cudaFree(dw);
+      }
+    }
   }
   cudaFree(bx);
   cudaFree(by);

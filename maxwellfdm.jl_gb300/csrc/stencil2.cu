@@ -211,9 +211,20 @@ __global__ void __launch_bounds__(V2<R, RW, NS, EDR>::NT, MB)
   pdl_trigger();
 
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TYT;
-  const int k0 = blockIdx.z * ex.kchunk;
-  const int k1 = min(k0 + ex.kchunk, a.N[2]);
+  // the block's column (x tile, y tile) and planes [k0, k1): uniform
+  // chunks of ex.kchunk planes, or an entry of the balanced schedule
+  int bx = blockIdx.x, by = blockIdx.y, k0 = blockIdx.z * ex.kchunk, k1;
+  if (ex.work != nullptr) {
+    const int4 wk = ex.work[blockIdx.x];
+    bx = wk.x;
+    by = wk.y;
+    k0 = wk.z;
+    k1 = wk.w;
+  } else {
+    k1 = min(k0 + ex.kchunk, a.N[2]);
+  }
+  const int tiles_x = (a.N[0] + TX - 1) / TX;
+  const int i0 = bx * TX, j0 = by * TYT;
   const int kfirst = k0 - 1;
   const int gi = i0 + lane;
   const int cx = 6 * (i0 - G::XOFF), cy = j0 - 1;
@@ -283,8 +294,8 @@ __global__ void __launch_bounds__(V2<R, RW, NS, EDR>::NT, MB)
         const int tr = j0 / RW + s;
         unsigned char f = 0;
         if (a.eoff != nullptr && q >= 0 && q < a.N[2] && tr < tiles_yr) {
-          if (ex.oflag_w != nullptr) f = ex.oflag_w[(blockIdx.x + (long long)gridDim.x * tr) * a.N[2] + q];
-          else if (a.oflag != nullptr) f = a.oflag[(blockIdx.x + (long long)gridDim.x * ((tr * RW) / 8)) * a.N[2] + q];
+          if (ex.oflag_w != nullptr) f = ex.oflag_w[(bx + (long long)tiles_x * tr) * a.N[2] + q];
+          else if (a.oflag != nullptr) f = a.oflag[(bx + (long long)tiles_x * ((tr * RW) / 8)) * a.N[2] + q];
           else f = 1;
         }
         zf[t * NW + s] = f;
@@ -772,6 +783,11 @@ static int launch_v2_t(fdfd_handle *h, const typename CT<R>::C *x, typename CT<R
   Extra<R> ex = make_extra<R>(h);
   ex.kchunk = kc;
   dim3 grid((h->N[0] + TX - 1) / TX, (h->N[1] + G::TYT - 1) / G::TYT, (h->N[2] + kc - 1) / kc);
+  const int p = sizeof(R) == 4 ? 1 : 0;
+  if (h->nwork[p] > 0) {  // the balanced schedule (built for this layout's tile rows)
+    ex.work = h->work[p];
+    grid = dim3((unsigned)h->nwork[p], 1, 1);
+  }
   if (EPI != EPI_STORE) {
     int rc = ensure_red(h, (int)(grid.x * grid.y * grid.z));
     if (rc) return rc;

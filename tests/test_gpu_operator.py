@@ -217,3 +217,29 @@ def test_forced_z_chunks(pkg, oracle, monkeypatch, kc, kernel):
     assert np.linalg.norm(A.matvec(x, "c128") - ref) / np.linalg.norm(ref) <= TOL64
     assert np.linalg.norm(A.matvec(x, "c64") - ref) / np.linalg.norm(ref) <= TOL32
     A.close()
+
+
+@pytest.mark.parametrize("waves", [1, 2, 4])
+@pytest.mark.parametrize("kernel", ["tma2", "tma2_1row"])
+def test_balanced_schedules(pkg, oracle, monkeypatch, waves, kernel):
+    """The second TMA kernel on a balanced z-chunk schedule (columns cut at
+    even estimated cost, planes with off-diagonal terms weighing more,
+    heaviest chunk first) gives the oracle's A x, and a mixed-precision solve
+    through it (reducing epilogues on a one-dimensional grid of schedule
+    entries) meets its tolerance on the oracle's matrix."""
+    monkeypatch.setenv("FDFD_OPERATOR_V2", {"tma2": "4", "tma2_1row": "1"}[kernel])
+    monkeypatch.setenv("FDFD_SCHEDULE", str(waves))
+    g = oracle.uniform_grid((64, 48, 70))
+    objs = [oracle.Sphere((20.0, 12.0, 30.0), 6.3, 12.25), oracle.Sphere((44.0, 30.0, 52.0), 4.1, 2.25)]
+    S = oracle.System(g, 2 * np.pi / 10, ((5, 5, 5), (5, 5, 5)), objs)
+    S.add_pointsrc((31.0, 23.0, 35.0), (0, 0, 1))
+    A = _make_op(pkg, S)
+    x = _rand(A.n, 31)
+    ref = S.A @ x
+    assert np.linalg.norm(A.matvec(x, "c128") - ref) / np.linalg.norm(ref) <= TOL64
+    assert np.linalg.norm(A.matvec(x, "c64") - ref) / np.linalg.norm(ref) <= TOL32
+    b = S.b()
+    xs, st = A.solve(b, tol=1e-7, precision="mixed")
+    assert st[0]["status"] == 0
+    assert np.linalg.norm(b - S.A @ xs) / np.linalg.norm(b) <= 1.02e-7
+    A.close()
