@@ -188,12 +188,13 @@ int fdfd_residual_dev(fdfd_handle *h, const void *x, const void *b, void *r, dou
  * counterpart in the reference (which never touches a GPU).  The call
  * allocates nothing: its reduction scratch (block partials, arrival counter,
  * result) is a fixed 512 KiB static device array that every GPU loading the
- * library holds until process exit.  It is synchronous: it returns once
- * rnorm2 is on the host.  Limits: the scratch holds 16384 thread-block
+ * library holds until process exit.  It is synchronous — it returns once
+ * rnorm2 is on the host — so it cannot be captured into a CUDA graph.  Limits: the scratch holds 16384 thread-block
  * partials; the z-chunk is lengthened as needed, so only grids whose x-y
  * tiling ⌈Nx/32⌉·⌈Ny/8⌉ exceeds 16384 (more than about 2048×2048 cells per
  * z-plane) are rejected with FDFD_ERR_ARG.  The first call on a device looks
- * up the array's device address (make it before any stream capture).  All
+ * up the array's device address (make it while no other stream of the
+ * process is capturing).  All
  * calls share the array: calls that overlap on the GPU race, so serialise
  * them. */
 int fdfd_residual_dev_noalloc(fdfd_handle *h, const void *x, const void *b, void *r, double *rnorm2);
