@@ -458,9 +458,14 @@ def run_profile(args):
         dt = torch.float32 if prec == "c64" else torch.float64
         x = torch.randn(A.n, 2, device=dev, dtype=dt)
         y = torch.empty_like(x)
+        A.sync()
+        # an NVTX range around the timed applications, so that a profiler can
+        # skip the autotuner's launches (ncu --nvtx --nvtx-include "matvec/")
+        torch.cuda.nvtx.range_push("matvec")
         for _ in range(args.reps):
             A.matvec_dev(x.data_ptr(), y.data_ptr(), prec)
         A.sync()
+        torch.cuda.nvtx.range_pop()
         print(f"profile matvec {N} {prec} x{args.reps} done")
     else:
         mdl, om = pkg.workloads.config2()
