@@ -1152,14 +1152,16 @@ int autotune_kchunk(fdfd_handle *h) {
       const char *fs = std::getenv("FDFD_SCHEDULE");
       const int forced = fs != nullptr ? std::atoi(fs) : -1;
       std::vector<std::vector<int4>> scheds;
-      std::vector<double> weights;
+      std::vector<std::pair<int, double>> labels;  // (waves, corner weight)
+      // corner-plane weights 0.25 … 1 for one and two waves, 1 beyond
       for (int waves = 1; waves <= 4; ++waves)
-        for (const double wc : {0.5, 1.0}) {
-          if (!h->has_off && wc != 0.5) continue;  // no corner terms: one weight is enough
+        for (const double wc : {0.25, 0.5, 1.0}) {
+          if (!h->has_off && wc != 1.0) continue;  // no corner terms: one weight is enough
+          if (waves > 2 && wc != 1.0) continue;
           if (forced >= 0 && (waves != forced || wc != 1.0)) continue;
           scheds.emplace_back();
           build_schedule(h, flags, rw, waves * slots, h->has_off ? wc : 0.0, scheds.back());
-          weights.push_back(waves + 0.1 * wc);
+          labels.push_back({waves, h->has_off ? wc : 0.0});
         }
       // a schedule must hold every column's planes once, in chunks of 1 …
       // KCMAX planes; one that does not is dropped (uniform chunks stay)
@@ -1176,7 +1178,7 @@ int autotune_kchunk(fdfd_handle *h) {
           if (bad || planes != (long long)ncol * h->N[2]) {
             if (verbose) fprintf(stderr, "fdfd autotune: schedule %zu dropped (bad chunks)\n", c);
             scheds.erase(scheds.begin() + c);
-            weights.erase(weights.begin() + c);
+            labels.erase(labels.begin() + c);
             --c;
           }
         }
@@ -1198,8 +1200,9 @@ int autotune_kchunk(fdfd_handle *h) {
         float med = 0.f;
         if ((rc = timed(&med))) break;
         if (verbose)
-          fprintf(stderr, "fdfd autotune: %s layout %d schedule %.1f (%zu blocks): %.1f us\n", prec ? "c64" : "c128",
-                  h->op_variant, weights[c], scheds[c].size(), med * 1e3);
+          fprintf(stderr, "fdfd autotune: %s layout %d schedule %d waves, weight %.2f (%zu blocks): %.1f us\n",
+                  prec ? "c64" : "c128", h->op_variant, labels[c].first, labels[c].second, scheds[c].size(),
+                  med * 1e3);
         if (med < 0.97f * best || forced > 0) {
           best = med;
           won = (int)c;
