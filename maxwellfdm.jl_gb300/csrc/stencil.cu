@@ -1109,6 +1109,12 @@ int autotune_kchunk(fdfd_handle *h) {
     if ((rc = cuda_check(h, cudaGetLastError(), "k_fill_hash"))) break;
     float best = 1e30f;
     int best_kc = 0, best_layout = h->op_variant;
+    std::vector<int4> best_sched;  // empty: uniform chunks
+    int4 *dw = nullptr;            // device copy of the schedule being timed
+    size_t dw_cap = 0;
+    // FDFD_SCHEDULE=w takes the w-wave schedule (weight 1) untimed, 0 none
+    const char *fs = std::getenv("FDFD_SCHEDULE");
+    const int forced = fs != nullptr ? std::atoi(fs) : -1;
     const int nlay = (prec == 1 && tune_layout) ? 3 : 1;
     for (int li = 0; li < nlay && rc == FDFD_OK; ++li) {
       if (prec == 1 && tune_layout) h->op_variant = layouts_c64[li];
@@ -1126,19 +1132,17 @@ int autotune_kchunk(fdfd_handle *h) {
                   kc, med * 1e3);
         // candidates come in increasing kc (fewer CTAs) and the default
         // layout first: take a later one only if it is clearly faster
-        if (med < 0.97f * best) {
+        if (med < 0.97f * best && forced <= 0) {
           best = med;
           best_kc = kc;
           best_layout = h->op_variant;
+          best_sched.clear();
         }
       }
-    }
-    h->kc[prec] = best_kc;
-    if (prec == 1 && tune_layout) h->op_variant = best_layout;
-    // the second TMA kernel can also run a balanced schedule: columns cut
-    // into chunks of equal estimated cost (planes with off-diagonal terms
-    // weigh more), for one to four waves of thread blocks
-    if (rc == FDFD_OK && best_kc > 0 && h->op_variant != 0) {
+      // the second TMA kernel can also run a balanced schedule of this
+      // layout: columns cut into chunks of equal estimated cost (planes with
+      // off-diagonal terms weigh more), for one to four waves of blocks
+      if (rc != FDFD_OK || h->op_variant == 0 || forced == 0) continue;
       const int rw = v2_rows_per_warp(h, prec == 1);
       std::vector<uint8_t> flags;
       if (h->has_off && h->oflag_rows[rw - 1] != nullptr) {
@@ -1148,75 +1152,74 @@ int autotune_kchunk(fdfd_handle *h) {
         if (rc == FDFD_OK) rc = cuda_check(h, cudaStreamSynchronize(h->stream), "stream sync");
       }
       const int slots = sms * ((prec == 1 && h->op_variant == 1) ? 3 : 2);
-      // FDFD_SCHEDULE=w takes the w-wave schedule (weight 1) untimed, 0 none
-      const char *fs = std::getenv("FDFD_SCHEDULE");
-      const int forced = fs != nullptr ? std::atoi(fs) : -1;
-      std::vector<std::vector<int4>> scheds;
-      std::vector<std::pair<int, double>> labels;  // (waves, corner weight)
+      const int tyt = 8 * rw;
+      const int ncol = ((h->N[0] + TX - 1) / TX) * ((h->N[1] + tyt - 1) / tyt);
       // corner-plane weights 0.25 … 1 for one and two waves, 1 beyond
-      for (int waves = 1; waves <= 4; ++waves)
+      for (int waves = 1; waves <= 4 && rc == FDFD_OK; ++waves)
         for (const double wc : {0.25, 0.5, 1.0}) {
+          if (rc != FDFD_OK) break;
           if (!h->has_off && wc != 1.0) continue;  // no corner terms: one weight is enough
           if (waves > 2 && wc != 1.0) continue;
-          if (forced >= 0 && (waves != forced || wc != 1.0)) continue;
-          scheds.emplace_back();
-          build_schedule(h, flags, rw, waves * slots, h->has_off ? wc : 0.0, scheds.back());
-          labels.push_back({waves, h->has_off ? wc : 0.0});
-        }
-      // a schedule must hold every column's planes once, in chunks of 1 …
-      // KCMAX planes; one that does not is dropped (uniform chunks stay)
-      {
-        const int tyt = 8 * rw;
-        const int ncol = ((h->N[0] + TX - 1) / TX) * ((h->N[1] + tyt - 1) / tyt);
-        for (size_t c = 0; c < scheds.size(); ++c) {
+          if (forced > 0 && (waves != forced || wc != 1.0)) continue;
+          std::vector<int4> sc;
+          build_schedule(h, flags, rw, waves * slots, h->has_off ? wc : 0.0, sc);
+          // every column's planes once, in chunks of 1 … KCMAX planes, or
+          // the schedule is not used
           long long planes = 0;
-          bool bad = scheds[c].empty();
-          for (const int4 &e : scheds[c]) {
+          bool bad = sc.empty();
+          for (const int4 &e : sc) {
             bad = bad || e.w <= e.z || e.w - e.z > KCMAX || e.z < 0 || e.w > h->N[2];
             planes += e.w - e.z;
           }
           if (bad || planes != (long long)ncol * h->N[2]) {
-            if (verbose) fprintf(stderr, "fdfd autotune: schedule %zu dropped (bad chunks)\n", c);
-            scheds.erase(scheds.begin() + c);
-            labels.erase(labels.begin() + c);
-            --c;
+            if (verbose) fprintf(stderr, "fdfd autotune: schedule dropped (bad chunks)\n");
+            continue;
+          }
+          if (sc.size() > dw_cap) {
+            cudaFree(dw);
+            dw = nullptr;
+            dw_cap = 0;
+            if (dev_malloc(&dw, sc.size() * sizeof(int4)) != cudaSuccess) {
+              cudaGetLastError();
+              rc = set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(schedule) failed");
+              break;
+            }
+            dw_cap = sc.size();
+          }
+          if ((rc = cuda_check(h, cudaMemcpyAsync(dw, sc.data(), sc.size() * sizeof(int4), cudaMemcpyHostToDevice,
+                                                  h->stream), "upload schedule")))
+            break;
+          h->work[prec] = dw;
+          h->nwork[prec] = (int)sc.size();
+          float med = 0.f;
+          rc = timed(&med);
+          h->work[prec] = nullptr;
+          h->nwork[prec] = 0;
+          if (rc) break;
+          if (verbose)
+            fprintf(stderr, "fdfd autotune: %s layout %d schedule %d waves, weight %.2f (%zu blocks): %.1f us\n",
+                    prec ? "c64" : "c128", h->op_variant, waves, h->has_off ? wc : 0.0, sc.size(), med * 1e3);
+          if (med < 0.97f * best || (forced > 0 && best_sched.empty())) {
+            best = med;
+            best_kc = h->kc[prec] > 0 ? h->kc[prec] : 4;
+            best_layout = h->op_variant;
+            best_sched = sc;
           }
         }
-      }
-      size_t cap = 0;
-      for (const auto &sc : scheds) cap = std::max(cap, sc.size());
-      int4 *dw = nullptr;
-      if (rc == FDFD_OK && dev_malloc(&dw, cap * sizeof(int4)) != cudaSuccess) {
+    }
+    cudaFree(dw);
+    h->kc[prec] = best_kc;
+    if (prec == 1 && tune_layout) h->op_variant = best_layout;
+    if (rc == FDFD_OK && !best_sched.empty()) {
+      int4 *w = nullptr;
+      if (dev_malloc(&w, best_sched.size() * sizeof(int4)) != cudaSuccess) {
         cudaGetLastError();
         rc = set_error(h, FDFD_ERR_NOMEM, "cudaMalloc(schedule) failed");
-      }
-      int won = -1;
-      for (size_t c = 0; c < scheds.size() && rc == FDFD_OK; ++c) {
-        rc = cuda_check(h, cudaMemcpyAsync(dw, scheds[c].data(), scheds[c].size() * sizeof(int4),
-                                           cudaMemcpyHostToDevice, h->stream), "upload schedule");
-        if (rc) break;
-        h->work[prec] = dw;
-        h->nwork[prec] = (int)scheds[c].size();
-        float med = 0.f;
-        if ((rc = timed(&med))) break;
-        if (verbose)
-          fprintf(stderr, "fdfd autotune: %s layout %d schedule %d waves, weight %.2f (%zu blocks): %.1f us\n",
-                  prec ? "c64" : "c128", h->op_variant, labels[c].first, labels[c].second, scheds[c].size(),
-                  med * 1e3);
-        if (med < 0.97f * best || forced > 0) {
-          best = med;
-          won = (int)c;
-        }
-      }
-      if (rc == FDFD_OK && won >= 0) {
-        rc = cuda_check(h, cudaMemcpyAsync(dw, scheds[won].data(), scheds[won].size() * sizeof(int4),
-                                           cudaMemcpyHostToDevice, h->stream), "upload schedule");
-        h->work[prec] = dw;
-        h->nwork[prec] = (int)scheds[won].size();
       } else {
-        h->work[prec] = nullptr;
-        h->nwork[prec] = 0;
-        cudaFree(dw);
+        rc = cuda_check(h, cudaMemcpyAsync(w, best_sched.data(), best_sched.size() * sizeof(int4),
+                                           cudaMemcpyHostToDevice, h->stream), "upload schedule");
+        h->work[prec] = w;
+        h->nwork[prec] = (int)best_sched.size();
       }
     }
   }
